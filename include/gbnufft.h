@@ -1,0 +1,168 @@
+/*
+ * gbnufft — C ABI of the GB300 NUFFT library (libgbnufft.so).
+ *
+ * This is the boundary that replaces the raw-plan layer of mri-nufft
+ * (RawFinufftPlan, src/mrinufft/operators/interfaces/finufft.py:23-80, and
+ * RawCufinufftPlan, src/mrinufft/operators/interfaces/cufinufft.py:51-137)
+ * together with the per-coil Python loops above it
+ * (src/mrinufft/operators/base.py:949-1139 and
+ * src/mrinufft/operators/interfaces/cufinufft.py:357-1178).
+ *
+ * Conventions
+ *  - every array argument is a device pointer (CUDA global memory) owned by
+ *    the caller, complex data is interleaved complex64 (float re, float im),
+ *    images are C-ordered with image axis d paired with sample coordinate d;
+ *  - sample coordinates are float32 radians in [-pi, pi) (values outside are
+ *    folded periodically), one array per image axis;
+ *  - type 2 ("op"):  y_j = scale * sum_n x_n exp(isign * i k_j . n)
+ *    type 1 ("adj"): x_n = scale * sum_j c_j exp(isign * i k_j . n)
+ *    with n in [-floor(N/2), N - floor(N/2)) per axis;
+ *  - every call is asynchronous on `stream` except gbn_setpts, which
+ *    synchronises `stream` once to size its work table;
+ *  - no C++ exception crosses this interface: each call returns a status
+ *    code (GBN_OK == 0) and gbn_last_error() describes the last failure of
+ *    the calling thread;
+ *  - a plan is not thread-safe; concurrent calls on one plan race.
+ */
+#ifndef GBNUFFT_H
+#define GBNUFFT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbn_plan_s* gbn_plan;
+/* Layout-compatible with cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* gbn_stream;
+
+#define GBN_OK 0
+#define GBN_ERR_ARG 1     /* invalid argument (shape, pointer, size) */
+#define GBN_ERR_CUDA 2    /* CUDA runtime error */
+#define GBN_ERR_CUFFT 3   /* cuFFT error */
+#define GBN_ERR_NOMEM 4   /* device allocation failed */
+#define GBN_ERR_STATE 5   /* call out of order (e.g. exec before setpts) */
+
+/* Library version as 10000*major + 100*minor + patch. */
+int gbn_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* gbn_last_error(void);
+
+/*
+ * Create a plan for `dim`-dimensional (2 or 3) transforms of image shape
+ * n_modes[0..dim-1].  Replaces finufft.Plan(2, shape, n_trans, eps, ...)
+ * (finufft.py:43-50) and cufinufft Plan(typ, shape, n_trans, eps, ...)
+ * (cufinufft.py:83-90).
+ *   upsampfac : fine-grid oversampling (2.0 in mri-nufft's default path)
+ *   eps       : requested relative accuracy (sets kernel width and shape)
+ *   ntrans    : transforms (coils) processed per pass; fine-grid memory is
+ *               ntrans * prod(nf) * 8 bytes
+ *   spread_only : 1 = only spread / interpolate on a grid of n_modes cells
+ *               with no FFT and no deapodisation (finufft's spreadinterponly,
+ *               used by the pipe density estimate, finufft.py:225-232)
+ *   device    : CUDA device ordinal the plan lives on
+ */
+int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double eps,
+                    int ntrans, int spread_only, int device, gbn_plan* out);
+
+/* Free a plan and its device memory. */
+int gbn_plan_destroy(gbn_plan plan);
+
+/* Kernel width, ES beta, fine grid nf[3] and bin sizes bins[3] of a plan
+ * (unused axes report 1). Any output pointer may be NULL. */
+int gbn_plan_info(gbn_plan plan, int* width, double* beta, int64_t* nf, int* bins);
+
+/* Device bytes currently held by the plan. */
+int gbn_plan_device_bytes(gbn_plan plan, int64_t* bytes);
+
+/*
+ * Set the non-uniform points: M samples, one float32 device array per image
+ * axis (k2 ignored in 2D).  Bin-sorts the points on the device.  Replaces
+ * Plan.setpts (finufft.py:55-62, cufinufft.py:94-113).
+ */
+int gbn_setpts(gbn_plan plan, int64_t M, const float* k0, const float* k1, const float* k2,
+               gbn_stream stream);
+
+/*
+ * Forward operator (type 2) for n_batchs x n_coils transforms, replacing
+ * FourierOperatorSimple.op/_op_sense/_op_calibless (base.py:949-1010) and
+ * MRICufiNUFFT._op_sense_device/_op_calibless_device (cufinufft.py:478-500,
+ * 609-620):
+ *   smaps != NULL (SENSE):  img (B, *N), smaps (C, *N), ksp (B, C, M),
+ *                            ksp[b, c] = scale * F(smaps[c] * img[b])
+ *   smaps == NULL:           img (B, C, *N), ksp (B, C, M)
+ * isign is -1 for mri-nufft's op and +1 for its trajectory-gradient plan.
+ */
+int gbn_op(gbn_plan plan, const void* img, const void* smaps, void* ksp, int n_batchs,
+           int n_coils, float scale, int isign, gbn_stream stream);
+
+/*
+ * Adjoint operator (type 1), replacing FourierOperatorSimple.adj_op /
+ * _adj_op_sense / _adj_op_calibless / _adj_op (base.py:1015-1073) and
+ * MRICufiNUFFT._adj_op_sense_device / _adj_op_calibless_device with the
+ * coil-combine kernel (cufinufft.py:743-770, gpu_utils.py:12-24):
+ *   density (M floats) may be NULL; it multiplies the k-space data;
+ *   smaps != NULL: ksp (B, C, M) -> img (B, *N) = scale * sum_c conj(smaps[c]) F^H(d ksp[b,c])
+ *   smaps == NULL: ksp (B, C, M) -> img (B, C, *N)
+ */
+int gbn_adj(gbn_plan plan, const void* ksp, const float* density, const void* smaps, void* img,
+            int n_batchs, int n_coils, float scale, int isign, gbn_stream stream);
+
+/*
+ * Data-consistency gradient A^H (A x - y), replacing
+ * FourierOperatorSimple.data_consistency / _grad_sense / _grad_calibless
+ * (base.py:1075-1139) and MRICufiNUFFT._dc_sense_device /
+ * _dc_calibless_device (cufinufft.py:1084-1178):
+ *   grad = scale * sum_c conj(s_c) F^H(d * (scale * F(s_c x) - y_c))
+ * with the same SENSE / calibrationless layouts as gbn_op / gbn_adj.
+ */
+int gbn_dc(gbn_plan plan, const void* img, const void* obs, const float* density,
+           const void* smaps, void* grad, int n_batchs, int n_coils, float scale,
+           gbn_stream stream);
+
+/*
+ * Pipe density iterations on a spread_only plan (one transform): `iters`
+ * times w <- w / |scale2 * interp(spread(w))|, with w complex64 of length M.
+ * Replaces the loop of MRIfinufft.pipe / MRICufiNUFFT.pipe
+ * (finufft.py:233-239, cufinufft.py:1319-1325).
+ */
+int gbn_pipe(gbn_plan plan, void* w, int iters, float scale2, gbn_stream stream);
+
+/*
+ * Trajectory gradient of the forward operator, replacing
+ * _backward_op_samples (operators/autodiff.py:22-41):
+ *   grad[j, d] = sum_{b,c} Re(conj(dy[b,c,j]) d/dk_{j,d} op(img)[b,c,j])
+ * evaluated with the derivative of the spreading kernel.  grad is (M, dim)
+ * float32 and is overwritten.  Layouts as gbn_op; dy as ksp.
+ */
+int gbn_grad_traj_op(gbn_plan plan, const void* img, const void* smaps, const void* dy,
+                     float* grad, int n_batchs, int n_coils, float scale, gbn_stream stream);
+
+/*
+ * Trajectory gradient of the adjoint operator, replacing
+ * _backward_adj_samples (operators/autodiff.py:69-86):
+ *   grad[j, d] = sum_{b,c} Re(y[b,c,j] d/dk_{j,d} op_+(conj(dx))[b,c,j])
+ * where op_+ is the isign=+1 forward operator with conjugated coil maps.
+ * dx has the image layout of gbn_op, y the k-space layout.
+ */
+int gbn_grad_traj_adj(gbn_plan plan, const void* dx, const void* smaps, const void* y,
+                      float* grad, int n_batchs, int n_coils, float scale, gbn_stream stream);
+
+/*
+ * FP64-accumulated reductions on complex64 vectors, used by the CG solver
+ * and the power method (extras/optim.py:872-878, base.py:1200-1206):
+ *   gbn_norm2_f64: out[0] = sum |x_i|^2
+ *   gbn_dotu_f64:  out[0] + i out[1] = sum a_i b_i  (conj_a: sum conj(a_i) b_i)
+ * `out` is a device pointer to doubles.
+ */
+int gbn_norm2_f64(const void* x, int64_t n, double* out, gbn_stream stream);
+int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* out,
+                 gbn_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBNUFFT_H */

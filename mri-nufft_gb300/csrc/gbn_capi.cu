@@ -1,0 +1,759 @@
+// C ABI of the GB300 NUFFT library: plans, point setting, operator calls.
+//
+// The pipelines (per pass of up to `ntrans` transforms):
+//   op  : pad pass (SENSE product, 1/phihat, zero pad) -> cuFFT -> interp
+//   adj : zero fine grid -> spread (density applied) -> cuFFT -> crop pass
+//         (1/phihat, scale, conj(smaps) coil sum)
+//   dc  : pad -> cuFFT -> interp with residual epilogue (scale*v - y)*d
+//         -> zero -> spread -> cuFFT -> crop (coil sum)
+//   pipe: zero -> spread -> interp with divide epilogue, on the N grid
+#include <cufft.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gbn_internal.cuh"
+#include "gbn_passes.cuh"
+#include "gbn_sort.cuh"
+#include "gbnufft.h"
+
+using namespace gbn;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Fail {
+  int code;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) {
+  g_err = msg;
+  throw Fail{code};
+}
+
+void ck(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    fail(GBN_ERR_NOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+  fail(GBN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void ckfft(cufftResult r, const char* what) {
+  if (r == CUFFT_SUCCESS) return;
+  if (r == CUFFT_ALLOC_FAILED) fail(GBN_ERR_NOMEM, std::string(what) + ": cuFFT allocation failed");
+  fail(GBN_ERR_CUFFT, std::string(what) + ": cuFFT error " + std::to_string((int)r));
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) ck(cudaSetDevice(dev), "cudaSetDevice");
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+template <typename T>
+T* dev_alloc(size_t count, int64_t& tally, const char* what) {
+  if (count == 0) count = 1;
+  void* p = nullptr;
+  ck(cudaMalloc(&p, count * sizeof(T)), what);
+  tally += (int64_t)(count * sizeof(T));
+  return static_cast<T*>(p);
+}
+
+void dev_free(void* p) {
+  if (p) cudaFree(p);
+}
+
+// ----------------------------------------------------------------------------
+// Kernel parameters (published exponential-of-semicircle rules of the finufft
+// paper, Barnett, Magland & af Klinteberg, SISC 2019, and the finufft docs):
+//   upsampfac 2: w = ceil(-log10(eps / 10)), beta = c(w) * w with
+//                c = 2.20, 2.26, 2.38 for w = 2, 3, 4 and 2.30 otherwise;
+//   other sigma: w = ceil(-ln(eps) / (pi sqrt(1 - 1/sigma))),
+//                beta = 0.97 * pi * w * (1 - 1 / (2 sigma));
+//   w is clamped to [2, 16].
+// ----------------------------------------------------------------------------
+void kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
+  int w;
+  double beta;
+  if (sigma == 2.0) {
+    w = (int)std::ceil(-std::log10(eps / 10.0));
+  } else {
+    w = (int)std::ceil(-std::log(eps) / (M_PI * std::sqrt(1.0 - 1.0 / sigma)));
+  }
+  if (w < 2) w = 2;
+  if (w > 16) w = 16;
+  if (sigma == 2.0) {
+    double c = 2.30;
+    if (w == 2) c = 2.20;
+    else if (w == 3) c = 2.26;
+    else if (w == 4) c = 2.38;
+    beta = c * w;
+  } else {
+    beta = 0.97 * M_PI * w * (1.0 - 1.0 / (2.0 * sigma));
+  }
+  *w_out = w;
+  *beta_out = beta;
+}
+
+// smallest even integer >= n with no prime factor other than 2, 3, 5
+int64_t next_smooth_even(int64_t n) {
+  if (n <= 2) return 2;
+  if (n % 2) ++n;
+  for (;; n += 2) {
+    int64_t r = n;
+    for (int p : {2, 3, 5})
+      while (r % p == 0) r /= p;
+    if (r == 1) return n;
+  }
+}
+
+// Gauss-Legendre nodes/weights on [-1, 1] (Newton on P_q, Golub-free)
+void gauss_legendre(int q, std::vector<double>& x, std::vector<double>& wts) {
+  x.assign(q, 0.0);
+  wts.assign(q, 0.0);
+  for (int i = 0; i < (q + 1) / 2; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (q + 0.5));
+    double pp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p1 = 1.0, p2 = 0.0;
+      for (int k = 1; k <= q; ++k) {
+        double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * k - 1.0) * z * p2 - (k - 1.0) * p3) / k;
+      }
+      pp = q * (z * p1 - p2) / (z * z - 1.0);
+      double z1 = z;
+      z = z1 - p1 / pp;
+      if (std::fabs(z - z1) < 1e-15) break;
+    }
+    x[i] = -z;
+    x[q - 1 - i] = z;
+    wts[i] = wts[q - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+  }
+}
+
+// 1 / phihat(n) for the N modes of one axis (array index i <-> mode i - N/2),
+// phihat(k) = int_{-w/2}^{w/2} phi(x) cos(2 pi k x / nf) dx in FP64.
+std::vector<float> deconv_factors(int N, int64_t nf, int w, double beta) {
+  std::vector<double> x, wt;
+  const int q = 2 * w + 48;
+  gauss_legendre(q, x, wt);
+  const double h = 0.5 * w;
+  std::vector<double> xs(q), fs(q);
+  for (int i = 0; i < q; ++i) {
+    xs[i] = h * x[i];
+    double z = xs[i] / h;
+    double t = 1.0 - z * z;
+    fs[i] = t > 0 ? std::exp(beta * (std::sqrt(t) - 1.0)) * h * wt[i] : 0.0;
+  }
+  std::vector<float> out(N);
+  for (int i = 0; i < N; ++i) {
+    double k = (double)(i - N / 2);
+    double s = 0.0;
+    for (int j = 0; j < q; ++j) s += fs[j] * std::cos(2.0 * M_PI * k * xs[j] / (double)nf);
+    out[i] = (float)(1.0 / s);
+  }
+  return out;
+}
+
+}  // namespace
+
+struct gbn_plan_s {
+  Geom g{};
+  int ntrans = 1;
+  int spread_only = 0;
+  int device = 0;
+  int nsm = 152;
+  double eps = 1e-6, sigma = 2.0, beta = 0.0;
+  int64_t bytes = 0;
+
+  float* dec[3] = {nullptr, nullptr, nullptr};
+  float2* fine = nullptr;
+  float2* kbuf = nullptr;  // ntrans x M residual scratch for dc
+  int64_t kbuf_cap = 0;
+
+  // sort state
+  int64_t M = -1, Mcap = 0, subcap = 0;
+  int maxsub = 256;
+  int nsub = 0;
+  SortBuffers sb{};
+  int nbins = 0;
+
+  std::map<int, cufftHandle> ffts;
+
+  ~gbn_plan_s() {
+    for (auto& kv : ffts) cufftDestroy(kv.second);
+    for (int d = 0; d < 3; ++d) dev_free(dec[d]);
+    dev_free(fine);
+    dev_free(kbuf);
+    free_points();
+    dev_free(sb.bin_count);
+    dev_free(sb.bin_start);
+    dev_free(sb.nsub_bin);
+    dev_free(sb.sub_off);
+    dev_free(sb.scan_scratch);
+    dev_free(sb.d_total);
+  }
+
+  void free_points() {
+    dev_free(sb.bin_of);
+    dev_free(sb.rank_of);
+    dev_free(sb.perm);
+    for (int d = 0; d < 3; ++d) dev_free(sb.u[d]);
+    dev_free(sb.sub_bin);
+    dev_free(sb.sub_start);
+    dev_free(sb.sub_count);
+    sb.bin_of = sb.rank_of = sb.perm = sb.sub_bin = sb.sub_start = sb.sub_count = nullptr;
+    sb.u[0] = sb.u[1] = sb.u[2] = nullptr;
+  }
+
+  Sorted sorted() const {
+    Sorted s{};
+    s.M = M;
+    s.perm = sb.perm;
+    for (int d = 0; d < 3; ++d) s.u[d] = sb.u[d];
+    s.sub_bin = sb.sub_bin;
+    s.sub_start = sb.sub_start;
+    s.sub_count = sb.sub_count;
+    s.nsub = nsub;
+    return s;
+  }
+
+  cufftHandle fft(int batch) {
+    auto it = ffts.find(batch);
+    if (it != ffts.end()) return it->second;
+    cufftHandle h;
+    int n[3];
+    for (int d = 0; d < g.dim; ++d) n[d] = g.nf[d];
+    ckfft(cufftPlanMany(&h, g.dim, n, nullptr, 1, (int)g.G, nullptr, 1, (int)g.G, CUFFT_C2C,
+                        batch),
+          "cufftPlanMany");
+    size_t ws = 0;
+    cufftGetSize(h, &ws);
+    bytes += (int64_t)ws;
+    ffts[batch] = h;
+    return h;
+  }
+
+  void exec_fft(int batch, float2* data, int isign, cudaStream_t st) {
+    cufftHandle h = fft(batch);
+    ckfft(cufftSetStream(h, st), "cufftSetStream");
+    ckfft(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data),
+                       reinterpret_cast<cufftComplex*>(data),
+                       isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE),
+          "cufftExecC2C");
+  }
+};
+
+namespace {
+
+void require_points(gbn_plan p) {
+  if (!p) fail(GBN_ERR_ARG, "null plan");
+  if (p->M < 0) fail(GBN_ERR_STATE, "gbn_setpts has not been called on this plan");
+}
+
+void launch_interp_dim(const InterpArgs& a, cudaStream_t st) {
+  ck(a.g.dim == 2 ? launch_interp2d(a, st) : launch_interp3d(a, st), "interp kernel");
+}
+void launch_spread_dim(const SpreadArgs& a, cudaStream_t st) {
+  ck(a.g.dim == 2 ? launch_spread2d(a, st) : launch_spread3d(a, st), "spread kernel");
+}
+
+PadArgs pad_args(gbn_plan p, const float2* img, const float2* smaps, int ntr, int conj_in) {
+  PadArgs a{};
+  a.g = p->g;
+  a.img = img;
+  a.smaps = smaps;
+  for (int d = 0; d < 3; ++d) a.dec[d] = p->dec[d];
+  a.fine = p->fine;
+  a.ntr = ntr;
+  a.conj_in = conj_in;
+  a.scale = 1.0f;
+  return a;
+}
+
+CropArgs crop_args(gbn_plan p, const float2* smaps, float2* out, int ntr, int accumulate,
+                   float scale) {
+  CropArgs a{};
+  a.g = p->g;
+  a.fine = p->fine;
+  a.smaps = smaps;
+  for (int d = 0; d < 3; ++d) a.dec[d] = p->dec[d];
+  a.out = out;
+  a.ntr = ntr;
+  a.accumulate = accumulate;
+  a.scale = scale;
+  return a;
+}
+
+InterpArgs interp_args(gbn_plan p, const float2* fine, float2* out, int ntr, float scale,
+                       int mode) {
+  InterpArgs a{};
+  a.g = p->g;
+  a.s = p->sorted();
+  a.fine = fine;
+  a.out = out;
+  a.ntr = ntr;
+  a.scale = scale;
+  a.mode = mode;
+  return a;
+}
+
+SpreadArgs spread_args(gbn_plan p, const float2* in, const float* density, float2* fine,
+                       int ntr, float scale) {
+  SpreadArgs a{};
+  a.g = p->g;
+  a.s = p->sorted();
+  a.in = in;
+  a.density = density;
+  a.fine = fine;
+  a.ntr = ntr;
+  a.scale = scale;
+  return a;
+}
+
+// Iterate transform passes.  SENSE: pass = (batch b, coils c0..c0+T);
+// calibrationless: pass = rows r0..r0+T of the flattened (B*C) stack.
+template <typename F>
+void for_each_pass(gbn_plan p, bool sense, int B, int C, F&& f) {
+  const int T = p->ntrans;
+  if (sense) {
+    for (int b = 0; b < B; ++b)
+      for (int c0 = 0; c0 < C; c0 += T) f(b, c0, imin(T, C - c0));
+  } else {
+    const int R = B * C;
+    for (int r0 = 0; r0 < R; r0 += T) f(-1, r0, imin(T, R - r0));
+  }
+}
+
+void check_counts(int B, int C) {
+  if (B < 1 || C < 1) fail(GBN_ERR_ARG, "n_batchs and n_coils must be >= 1");
+}
+
+template <typename F>
+int guarded(gbn_plan p, F&& f) {
+  try {
+    if (!p) fail(GBN_ERR_ARG, "null plan");
+    DeviceGuard dg(p->device);
+    f();
+    return GBN_OK;
+  } catch (const Fail& e) {
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return GBN_ERR_NOMEM;
+  } catch (...) {
+    g_err = "unexpected error";
+    return GBN_ERR_CUDA;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbn_version(void) { return 100; }
+
+const char* gbn_last_error(void) { return g_err.c_str(); }
+
+int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double eps, int ntrans,
+                    int spread_only, int device, gbn_plan* out) {
+  g_err.clear();
+  if (!out) {
+    g_err = "null output pointer";
+    return GBN_ERR_ARG;
+  }
+  *out = nullptr;
+  gbn_plan p = nullptr;
+  try {
+    if (dim != 2 && dim != 3) fail(GBN_ERR_ARG, "dim must be 2 or 3");
+    if (!n_modes) fail(GBN_ERR_ARG, "null n_modes");
+    if (!(eps > 0.0) || !(eps < 1.0)) fail(GBN_ERR_ARG, "eps must be in (0, 1)");
+    if (!(upsampfac > 1.0) && !spread_only) fail(GBN_ERR_ARG, "upsampfac must be > 1");
+    if (ntrans < 1) fail(GBN_ERR_ARG, "ntrans must be >= 1");
+    int ndev = 0;
+    ck(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) fail(GBN_ERR_ARG, "invalid device ordinal");
+    DeviceGuard dg(device);
+    p = new gbn_plan_s();
+    p->device = device;
+    p->ntrans = ntrans;
+    p->spread_only = spread_only ? 1 : 0;
+    p->eps = eps;
+    p->sigma = upsampfac;
+    cudaDeviceProp prop;
+    ck(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    p->nsm = prop.multiProcessorCount;
+    int w;
+    double beta;
+    kernel_params(eps, upsampfac > 1.0 ? upsampfac : 2.0, &w, &beta);
+    p->beta = beta;
+    Geom& g = p->g;
+    g.dim = dim;
+    g.w = w;
+    g.beta = (float)beta;
+    g.halfw = 0.5f * w;
+    g.inv_halfw = 2.0f / w;
+    g.G = 1;
+    g.Nimg = 1;
+    const int binsz2[2] = {32, 32};
+    const int binsz3[3] = {8, 8, 8};
+    for (int d = 0; d < 3; ++d) {
+      if (d < dim) {
+        int64_t N = n_modes[d];
+        if (N < 1 || N > (1 << 20)) fail(GBN_ERR_ARG, "image size out of range");
+        int64_t nf;
+        if (spread_only) nf = N;
+        else {
+          int64_t want = (int64_t)std::ceil(upsampfac * (double)N);
+          if (want < 2 * w) want = 2 * w;
+          nf = next_smooth_even(want);
+        }
+        g.n[d] = (int)N;
+        g.nf[d] = (int)nf;
+        int bs = dim == 2 ? binsz2[d] : binsz3[d];
+        if (bs > nf) bs = (int)nf;
+        g.bs[d] = bs;
+        g.nb[d] = (int)((nf + bs - 1) / bs);
+        g.pd[d] = bs + w;
+        g.uscale[d] = (float)((double)nf / (2.0 * M_PI));
+      } else {
+        g.n[d] = g.nf[d] = g.bs[d] = g.nb[d] = g.pd[d] = 1;
+        g.uscale[d] = 0.f;
+      }
+      g.G *= g.nf[d];
+      g.Nimg *= g.n[d];
+    }
+    if (g.G > ((int64_t)1 << 31) - 1) fail(GBN_ERR_ARG, "fine grid larger than 2^31 cells");
+    g.tile = g.pd[0] * g.pd[1] * g.pd[2];
+    if ((int64_t)g.tile * 8 > kTileSmemBudget) fail(GBN_ERR_ARG, "tile does not fit shared memory");
+    p->nbins = g.nb[0] * g.nb[1] * g.nb[2];
+
+    if (!spread_only) {
+      for (int d = 0; d < dim; ++d) {
+        std::vector<float> f = deconv_factors(g.n[d], g.nf[d], w, beta);
+        p->dec[d] = dev_alloc<float>(f.size(), p->bytes, "deconv factors");
+        ck(cudaMemcpy(p->dec[d], f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice),
+           "copy deconv factors");
+      }
+    }
+    p->fine = dev_alloc<float2>((size_t)ntrans * g.G, p->bytes, "fine grid");
+    p->sb.bin_count = dev_alloc<int>(p->nbins, p->bytes, "bins");
+    p->sb.bin_start = dev_alloc<int>(p->nbins, p->bytes, "bins");
+    p->sb.nsub_bin = dev_alloc<int>(p->nbins, p->bytes, "bins");
+    p->sb.sub_off = dev_alloc<int>(p->nbins, p->bytes, "bins");
+    p->sb.scan_scratch = dev_alloc<int>(scan_scratch_ints(p->nbins), p->bytes, "scan");
+    p->sb.d_total = dev_alloc<int>(1, p->bytes, "scan");
+    *out = p;
+    return GBN_OK;
+  } catch (const Fail& e) {
+    delete p;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    delete p;
+    g_err = "host allocation failed";
+    return GBN_ERR_NOMEM;
+  }
+}
+
+int gbn_plan_destroy(gbn_plan plan) {
+  if (!plan) return GBN_OK;
+  int dev = plan->device;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != dev) cudaSetDevice(dev);
+  delete plan;
+  if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+  return GBN_OK;
+}
+
+int gbn_plan_info(gbn_plan p, int* width, double* beta, int64_t* nf, int* bins) {
+  if (!p) {
+    g_err = "null plan";
+    return GBN_ERR_ARG;
+  }
+  if (width) *width = p->g.w;
+  if (beta) *beta = p->beta;
+  for (int d = 0; d < 3; ++d) {
+    if (nf) nf[d] = p->g.nf[d];
+    if (bins) bins[d] = p->g.bs[d];
+  }
+  return GBN_OK;
+}
+
+int gbn_plan_device_bytes(gbn_plan p, int64_t* bytes) {
+  if (!p || !bytes) {
+    g_err = "null argument";
+    return GBN_ERR_ARG;
+  }
+  *bytes = p->bytes;
+  return GBN_OK;
+}
+
+int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const float* k2,
+               gbn_stream stream) {
+  return guarded(p, [&] {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (M < 0 || M > ((int64_t)1 << 31) - 1) fail(GBN_ERR_ARG, "M out of range");
+    if (M > 0 && (!k0 || !k1 || (p->g.dim == 3 && !k2))) fail(GBN_ERR_ARG, "null coordinates");
+    // subproblem size: aim at >= 4 subproblems per SM, 32..1024 samples
+    int64_t target = M / (4 * (int64_t)p->nsm);
+    int maxsub = 32;
+    while (maxsub < target && maxsub < 1024) maxsub <<= 1;
+    int64_t subcap = M / maxsub + (M < p->nbins ? M : p->nbins) + 1;
+    if (M > p->Mcap || subcap > p->subcap) {
+      // free the previous point buffers before the new ones (bytes tally)
+      int64_t old = 0;
+      if (p->sb.perm) old = p->Mcap * (int64_t)(4 * 3 + 4 * p->g.dim) + p->subcap * 12;
+      p->free_points();
+      p->bytes -= old;
+      int64_t cap = M > p->Mcap ? M : p->Mcap;
+      int64_t scap = subcap > p->subcap ? subcap : p->subcap;
+      p->sb.bin_of = dev_alloc<int>(cap, p->bytes, "sort scratch");
+      p->sb.rank_of = dev_alloc<int>(cap, p->bytes, "sort scratch");
+      p->sb.perm = dev_alloc<int>(cap, p->bytes, "permutation");
+      for (int d = 0; d < p->g.dim; ++d) p->sb.u[d] = dev_alloc<float>(cap, p->bytes, "coords");
+      p->sb.sub_bin = dev_alloc<int>(scap, p->bytes, "subproblems");
+      p->sb.sub_start = dev_alloc<int>(scap, p->bytes, "subproblems");
+      p->sb.sub_count = dev_alloc<int>(scap, p->bytes, "subproblems");
+      p->Mcap = cap;
+      p->subcap = scap;
+    }
+    const float* k[3] = {k0, k1, k2};
+    p->maxsub = maxsub;
+    ck(sort_points(p->g, M, k, maxsub, p->sb, st), "sort");
+    int total = 0;
+    ck(cudaMemcpyAsync(&total, p->sb.d_total, sizeof(int), cudaMemcpyDeviceToHost, st),
+       "copy subproblem count");
+    ck(cudaStreamSynchronize(st), "setpts sync");
+    if (total > p->subcap) fail(GBN_ERR_CUDA, "subproblem table overflow");
+    p->nsub = total;
+    p->M = M;
+  });
+}
+
+int gbn_op(gbn_plan p, const void* img, const void* smaps, void* ksp, int B, int C,
+           float scale, int isign, gbn_stream stream) {
+  return guarded(p, [&] {
+    require_points(p);
+    check_counts(B, C);
+    if (!img || (!ksp && p->M > 0)) fail(GBN_ERR_ARG, "null image or k-space pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const float2* x = static_cast<const float2*>(img);
+    const float2* s = static_cast<const float2*>(smaps);
+    float2* y = static_cast<float2*>(ksp);
+    const Geom& g = p->g;
+    if (p->spread_only) {
+      if (s) fail(GBN_ERR_ARG, "coil maps are not supported on a spread-only plan");
+      // the image array is the fine grid
+      for (int r0 = 0; r0 < B * C; r0 += p->ntrans) {
+        int T = imin(p->ntrans, B * C - r0);
+        launch_interp_dim(interp_args(p, x + (int64_t)r0 * g.G, y + (int64_t)r0 * p->M, T,
+                                      scale, INTERP_STORE), st);
+      }
+      return;
+    }
+    for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
+      PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
+                     : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
+      ck(launch_pad(pa, st), "pad pass");
+      p->exec_fft(T, p->fine, isign, st);
+      int64_t row = s ? (int64_t)b * C + c0 : c0;
+      launch_interp_dim(interp_args(p, p->fine, y + row * p->M, T, scale, INTERP_STORE), st);
+    });
+  });
+}
+
+int gbn_adj(gbn_plan p, const void* ksp, const float* density, const void* smaps, void* img,
+            int B, int C, float scale, int isign, gbn_stream stream) {
+  return guarded(p, [&] {
+    require_points(p);
+    check_counts(B, C);
+    if (!img || (!ksp && p->M > 0)) fail(GBN_ERR_ARG, "null image or k-space pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const float2* y = static_cast<const float2*>(ksp);
+    const float2* s = static_cast<const float2*>(smaps);
+    float2* x = static_cast<float2*>(img);
+    const Geom& g = p->g;
+    if (p->spread_only) {
+      if (s) fail(GBN_ERR_ARG, "coil maps are not supported on a spread-only plan");
+      for (int r0 = 0; r0 < B * C; r0 += p->ntrans) {
+        int T = imin(p->ntrans, B * C - r0);
+        float2* dst = x + (int64_t)r0 * g.G;
+        ck(cudaMemsetAsync(dst, 0, sizeof(float2) * (size_t)T * g.G, st), "zero grid");
+        launch_spread_dim(spread_args(p, y + (int64_t)r0 * p->M, density, dst, T, scale), st);
+      }
+      return;
+    }
+    for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
+      ck(cudaMemsetAsync(p->fine, 0, sizeof(float2) * (size_t)T * g.G, st), "zero grid");
+      int64_t row = s ? (int64_t)b * C + c0 : c0;
+      launch_spread_dim(spread_args(p, y + row * p->M, density, p->fine, T, 1.0f), st);
+      p->exec_fft(T, p->fine, isign, st);
+      CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, x + (int64_t)b * g.Nimg, T,
+                                  c0 > 0, scale)
+                      : crop_args(p, nullptr, x + (int64_t)c0 * g.Nimg, T, 0, scale);
+      ck(launch_crop(ca, st), "crop pass");
+    });
+  });
+}
+
+int gbn_dc(gbn_plan p, const void* img, const void* obs, const float* density,
+           const void* smaps, void* grad, int B, int C, float scale, gbn_stream stream) {
+  return guarded(p, [&] {
+    require_points(p);
+    check_counts(B, C);
+    if (p->spread_only) fail(GBN_ERR_ARG, "data consistency needs a full NUFFT plan");
+    if (!img || !grad || (!obs && p->M > 0)) fail(GBN_ERR_ARG, "null pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const float2* x = static_cast<const float2*>(img);
+    const float2* yo = static_cast<const float2*>(obs);
+    const float2* s = static_cast<const float2*>(smaps);
+    float2* gr = static_cast<float2*>(grad);
+    const Geom& g = p->g;
+    int64_t need = (int64_t)p->ntrans * (p->M > 0 ? p->M : 1);
+    if (need > p->kbuf_cap) {
+      dev_free(p->kbuf);
+      p->bytes -= p->kbuf_cap * 8;
+      p->kbuf = nullptr;
+      p->kbuf_cap = 0;
+      p->kbuf = dev_alloc<float2>(need, p->bytes, "residual buffer");
+      p->kbuf_cap = need;
+    }
+    for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
+      PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
+                     : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
+      ck(launch_pad(pa, st), "pad pass");
+      p->exec_fft(T, p->fine, -1, st);
+      int64_t row = s ? (int64_t)b * C + c0 : c0;
+      InterpArgs ia = interp_args(p, p->fine, p->kbuf, T, scale, INTERP_RESID);
+      ia.obs = yo + row * p->M;
+      ia.density = density;
+      launch_interp_dim(ia, st);
+      ck(cudaMemsetAsync(p->fine, 0, sizeof(float2) * (size_t)T * g.G, st), "zero grid");
+      launch_spread_dim(spread_args(p, p->kbuf, nullptr, p->fine, T, 1.0f), st);
+      p->exec_fft(T, p->fine, +1, st);
+      CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, gr + (int64_t)b * g.Nimg, T,
+                                  c0 > 0, scale)
+                      : crop_args(p, nullptr, gr + (int64_t)c0 * g.Nimg, T, 0, scale);
+      ck(launch_crop(ca, st), "crop pass");
+    });
+  });
+}
+
+int gbn_pipe(gbn_plan p, void* w, int iters, float scale2, gbn_stream stream) {
+  return guarded(p, [&] {
+    require_points(p);
+    if (!p->spread_only) fail(GBN_ERR_ARG, "pipe needs a spread-only plan");
+    if (!w && p->M > 0) fail(GBN_ERR_ARG, "null weights");
+    if (iters < 0) fail(GBN_ERR_ARG, "iters must be >= 0");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    float2* wv = static_cast<float2*>(w);
+    const Geom& g = p->g;
+    for (int it = 0; it < iters; ++it) {
+      ck(cudaMemsetAsync(p->fine, 0, sizeof(float2) * (size_t)g.G, st), "zero grid");
+      launch_spread_dim(spread_args(p, wv, nullptr, p->fine, 1, 1.0f), st);
+      launch_interp_dim(interp_args(p, p->fine, wv, 1, scale2, INTERP_PIPE), st);
+    }
+  });
+}
+
+static void grad_traj_common(gbn_plan p, const float2* img, const float2* s, const float2* a,
+                             float* grad, int B, int C, float scale, int adjoint,
+                             cudaStream_t st) {
+  const Geom& g = p->g;
+  if (p->M > 0)
+    ck(cudaMemsetAsync(grad, 0, sizeof(float) * (size_t)p->M * g.dim, st), "zero gradient");
+  for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
+    PadArgs pa = s ? pad_args(p, img + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, adjoint)
+                   : pad_args(p, img + (int64_t)c0 * g.Nimg, nullptr, T, adjoint);
+    ck(launch_pad(pa, st), "pad pass");
+    p->exec_fft(T, p->fine, adjoint ? +1 : -1, st);
+    int64_t row = s ? (int64_t)b * C + c0 : c0;
+    GradArgs ga{};
+    ga.g = g;
+    ga.s = p->sorted();
+    ga.fine = p->fine;
+    ga.dy = a + row * p->M;
+    ga.grad = grad;
+    ga.ntr = T;
+    ga.scale = scale;
+    ga.conj_a = adjoint ? 0 : 1;
+    ck(g.dim == 2 ? launch_grad2d(ga, st) : launch_grad3d(ga, st), "gradient kernel");
+  });
+}
+
+int gbn_grad_traj_op(gbn_plan p, const void* img, const void* smaps, const void* dy,
+                     float* grad, int B, int C, float scale, gbn_stream stream) {
+  return guarded(p, [&] {
+    require_points(p);
+    check_counts(B, C);
+    if (p->spread_only) fail(GBN_ERR_ARG, "needs a full NUFFT plan");
+    if (!img || ((!dy || !grad) && p->M > 0)) fail(GBN_ERR_ARG, "null pointer");
+    grad_traj_common(p, static_cast<const float2*>(img), static_cast<const float2*>(smaps),
+                     static_cast<const float2*>(dy), grad, B, C, scale, 0,
+                     reinterpret_cast<cudaStream_t>(stream));
+  });
+}
+
+int gbn_grad_traj_adj(gbn_plan p, const void* dx, const void* smaps, const void* y, float* grad,
+                      int B, int C, float scale, gbn_stream stream) {
+  return guarded(p, [&] {
+    require_points(p);
+    check_counts(B, C);
+    if (p->spread_only) fail(GBN_ERR_ARG, "needs a full NUFFT plan");
+    if (!dx || ((!y || !grad) && p->M > 0)) fail(GBN_ERR_ARG, "null pointer");
+    grad_traj_common(p, static_cast<const float2*>(dx), static_cast<const float2*>(smaps),
+                     static_cast<const float2*>(y), grad, B, C, scale, 1,
+                     reinterpret_cast<cudaStream_t>(stream));
+  });
+}
+
+int gbn_norm2_f64(const void* x, int64_t n, double* out, gbn_stream stream) {
+  g_err.clear();
+  if ((!x && n > 0) || !out || n < 0) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  cudaError_t e = launch_norm2(static_cast<const float2*>(x), n, out,
+                               reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) {
+    g_err = cudaGetErrorString(e);
+    return GBN_ERR_CUDA;
+  }
+  return GBN_OK;
+}
+
+int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* out,
+                 gbn_stream stream) {
+  g_err.clear();
+  if (((!a || !b) && n > 0) || !out || n < 0) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  cudaError_t e = launch_dotu(static_cast<const float2*>(a), static_cast<const float2*>(b), n,
+                              conj_a, out, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) {
+    g_err = cudaGetErrorString(e);
+    return GBN_ERR_CUDA;
+  }
+  return GBN_OK;
+}
+
+}  // extern "C"

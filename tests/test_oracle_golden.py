@@ -1,0 +1,85 @@
+"""The CPU oracle against golden vectors produced by the reference itself.
+
+The fixtures in ``tests/golden/ndft_golden.npz`` were generated by
+``tests/golden/make_golden.py`` running mri-nufft's own FP64 NDFT backend
+(``MRInumpy``) on the reference's test trajectories.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from oracle import ndft
+from oracle.operator import NDFTOperator
+
+CASES = ["random2D", "random3D", "grid2D", "grid3D", "radial2D"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_ndft_matches_reference(golden, name):
+    s = golden[f"{name}__samples"]
+    shape = tuple(int(v) for v in golden[f"{name}__shape"])
+    su = ndft.proper_trajectory_unit(s)
+    nf = ndft.norm_factor(shape)
+    y = ndft.ndft_type2(su, golden[f"{name}__img"], shape) / nf
+    x = ndft.ndft_type1(su, golden[f"{name}__ksp"], shape) / nf
+    assert rel_l2(y, golden[f"{name}__op"]) < 1e-12
+    assert rel_l2(x, golden[f"{name}__adj"]) < 1e-12
+
+
+def test_ndft_subsets_match_full(golden):
+    s = ndft.proper_trajectory_unit(golden["random3D__samples"])
+    shape = tuple(int(v) for v in golden["random3D__shape"])
+    img, ksp = golden["random3D__img"], golden["random3D__ksp"]
+    rows = np.array([0, 5, 17, 1999])
+    full = ndft.ndft_type2(s, img, shape)
+    np.testing.assert_allclose(ndft.ndft_type2_rows(s, img, shape, rows), full[rows], rtol=1e-12)
+    vox = np.array([0, 7, 4000, 13311])
+    full1 = ndft.ndft_type1(s, ksp, shape).reshape(-1)
+    np.testing.assert_allclose(ndft.ndft_type1_voxels(s, ksp, shape, vox), full1[vox], rtol=1e-10)
+
+
+def test_ndft_grid_is_fft(golden):
+    # test_ndft.py:58-79 of the reference: NDFT on a Cartesian grid is an FFT
+    N = 16
+    s = golden["grid2D__samples"]
+    img = golden["grid2D__img"]
+    y = ndft.ndft_type2(ndft.proper_trajectory_unit(s), img, (N, N)).reshape(N, N)
+    ref = np.fft.fftn(np.fft.fftshift(img)).T  # meshgrid "xy" ordering swaps axes
+    np.testing.assert_allclose(y, ref, atol=1e-9, rtol=1e-9)
+
+
+def test_operator_sense_calib_dc(golden):
+    s = golden["sense__samples"]
+    shape = tuple(int(v) for v in golden["sense__shape"])
+    smaps = golden["sense__smaps"]
+    B, C = 2, smaps.shape[0]
+    op = NDFTOperator(s, shape, n_batchs=B, smaps=smaps)
+    assert rel_l2(op.op(golden["sense__img"]), golden["sense__op"]) < 1e-12
+    assert rel_l2(op.adj(golden["sense__ksp"]), golden["sense__adj"]) < 1e-12
+    assert rel_l2(op.dc(golden["sense__img"], golden["sense__ksp"]), golden["sense__dc"]) < 1e-12
+    opc = NDFTOperator(s, shape, n_coils=C, n_batchs=B)
+    assert rel_l2(opc.op(golden["calib__img"]), golden["calib__op"]) < 1e-12
+    assert rel_l2(opc.adj(golden["sense__ksp"]), golden["calib__adj"]) < 1e-12
+    assert rel_l2(opc.dc(golden["calib__img"], golden["sense__ksp"]), golden["calib__dc"]) < 1e-12
+
+
+def test_proper_trajectory_oracle(golden):
+    np.testing.assert_allclose(ndft.proper_trajectory_pi(golden["proper__unit_in"]),
+                               golden["proper__unit_to_pi"])
+    np.testing.assert_allclose(ndft.proper_trajectory_unit(golden["proper__unit_to_pi"]),
+                               golden["proper__pi_to_unit"])
+    np.testing.assert_allclose(ndft.proper_trajectory_unit(golden["proper__wrap_in"]),
+                               golden["proper__wrap_unit"])
+
+
+def test_odd_size_grids_differ_by_half_shift():
+    # the NDFT grid of the reference is linspace(-N/2, N/2-1, N): for odd N it
+    # is shifted by half a cell from the integer modes of finufft
+    k = np.array([[0.1, -0.2]])
+    x = np.zeros((5, 4), complex)
+    x[0, 0] = 1.0
+    a = ndft.ndft_type2(k, x, (5, 4), grid="ndft")
+    b = ndft.ndft_type2(k, x, (5, 4), grid="finufft")
+    # n0 = -2.5 vs -2
+    np.testing.assert_allclose(a / b, np.exp(-2j * np.pi * 0.1 * (-0.5)), rtol=1e-12)
