@@ -151,6 +151,27 @@ int gbn_grad_traj_adj(gbn_plan plan, const void* dx, const void* smaps, const vo
                       float* grad, int n_batchs, int n_coils, float scale, gbn_stream stream);
 
 /*
+ * Stage timing.  gbn_profile(plan, 1) clears the counters and records a pair
+ * of CUDA events on the launch stream around every launch of a stage;
+ * gbn_profile(plan, 0) stops recording.  gbn_profile_read waits for the
+ * recorded events and returns the summed device time and number of launches
+ * of one stage (GBN_STAGE_*), or with stage = -1 the time of all stages and
+ * the number of kernels this library launched through the plan since the
+ * last gbn_profile call.  No counterpart in the reference (which times
+ * nothing); it feeds the roofline figures of the benchmark.
+ */
+#define GBN_STAGE_PAD 0
+#define GBN_STAGE_FFT 1
+#define GBN_STAGE_INTERP 2
+#define GBN_STAGE_SPREAD 3
+#define GBN_STAGE_CROP 4
+#define GBN_STAGE_ZERO 5
+#define GBN_STAGE_GRAD 6
+#define GBN_STAGES 7
+int gbn_profile(gbn_plan plan, int enable);
+int gbn_profile_read(gbn_plan plan, int stage, double* total_ms, int64_t* count);
+
+/*
  * FP64-accumulated reductions on complex64 vectors, used by the CG solver
  * and the power method (extras/optim.py:872-878, base.py:1200-1206):
  *   gbn_norm2_f64: out[0] = sum |x_i|^2

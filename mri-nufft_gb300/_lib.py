@@ -25,6 +25,8 @@ GBN_ERR_CUFFT = 3
 GBN_ERR_NOMEM = 4
 GBN_ERR_STATE = 5
 
+STAGES = {"pad": 0, "fft": 1, "interp": 2, "spread": 3, "crop": 4, "zero": 5, "grad": 6}
+
 # name -> (restype, argtypes); must match include/gbnufft.h
 SIGNATURES = {
     "gbn_version": (_c_int, []),
@@ -46,6 +48,8 @@ SIGNATURES = {
     "gbn_pipe": (_c_int, [_vp, _vp, _c_int, _c_flt, _vp]),
     "gbn_grad_traj_op": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _vp]),
     "gbn_grad_traj_adj": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _vp]),
+    "gbn_profile": (_c_int, [_vp, _c_int]),
+    "gbn_profile_read": (_c_int, [_vp, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_i64)]),
     "gbn_norm2_f64": (_c_int, [_vp, _c_i64, _vp, _vp]),
     "gbn_dotu_f64": (_c_int, [_vp, _vp, _c_i64, _c_int, _vp, _vp]),
 }

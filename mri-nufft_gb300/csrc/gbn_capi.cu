@@ -197,7 +197,25 @@ struct gbn_plan_s {
 
   std::map<int, cufftHandle> ffts;
 
+  // per-stage CUDA-event timing (gbn_profile) and kernel launch count
+  bool prof = false;
+  std::vector<cudaEvent_t> evpool;
+  size_t evnext = 0;
+  std::vector<std::pair<size_t, size_t>> spans[GBN_STAGES];
+  int64_t launches = 0;
+
+  size_t record(cudaStream_t st) {
+    if (evnext == evpool.size()) {
+      cudaEvent_t e;
+      ck(cudaEventCreate(&e), "cudaEventCreate");
+      evpool.push_back(e);
+    }
+    ck(cudaEventRecord(evpool[evnext], st), "cudaEventRecord");
+    return evnext++;
+  }
+
   ~gbn_plan_s() {
+    for (auto e : evpool) cudaEventDestroy(e);
     for (auto& kv : ffts) cufftDestroy(kv.second);
     for (int d = 0; d < 3; ++d) dev_free(dec[d]);
     dev_free(fine);
@@ -251,15 +269,35 @@ struct gbn_plan_s {
     return h;
   }
 
-  void exec_fft(int batch, float2* data, int isign, cudaStream_t st) {
+  void exec_fft(int batch, float2* data, int isign, cudaStream_t st);
+};
+
+// Records CUDA events around one stage launch when profiling is enabled.
+struct Span {
+  gbn_plan_s* p;
+  int stage;
+  cudaStream_t st;
+  size_t a = (size_t)-1;
+  Span(gbn_plan_s* p_, int stage_, cudaStream_t st_) : p(p_), stage(stage_), st(st_) {
+    if (p->prof) a = p->record(st);
+  }
+  ~Span() {
+    if (a != (size_t)-1) {
+      size_t b = p->record(st);
+      p->spans[stage].push_back({a, b});
+    }
+  }
+};
+
+void gbn_plan_s::exec_fft(int batch, float2* data, int isign, cudaStream_t st) {
+    Span span(this, GBN_STAGE_FFT, st);
     cufftHandle h = fft(batch);
     ckfft(cufftSetStream(h, st), "cufftSetStream");
     ckfft(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data),
                        reinterpret_cast<cufftComplex*>(data),
                        isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE),
           "cufftExecC2C");
-  }
-};
+}
 
 namespace {
 
@@ -268,11 +306,37 @@ void require_points(gbn_plan p) {
   if (p->M < 0) fail(GBN_ERR_STATE, "gbn_setpts has not been called on this plan");
 }
 
-void launch_interp_dim(const InterpArgs& a, cudaStream_t st) {
+void run_interp(gbn_plan p, const InterpArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return;
+  Span span(p, GBN_STAGE_INTERP, st);
   ck(a.g.dim == 2 ? launch_interp2d(a, st) : launch_interp3d(a, st), "interp kernel");
+  p->launches++;
 }
-void launch_spread_dim(const SpreadArgs& a, cudaStream_t st) {
+void run_spread(gbn_plan p, const SpreadArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return;
+  Span span(p, GBN_STAGE_SPREAD, st);
   ck(a.g.dim == 2 ? launch_spread2d(a, st) : launch_spread3d(a, st), "spread kernel");
+  p->launches++;
+}
+void run_pad(gbn_plan p, const PadArgs& a, cudaStream_t st) {
+  Span span(p, GBN_STAGE_PAD, st);
+  ck(launch_pad(a, st), "pad pass");
+  p->launches++;
+}
+void run_crop(gbn_plan p, const CropArgs& a, cudaStream_t st) {
+  Span span(p, GBN_STAGE_CROP, st);
+  ck(launch_crop(a, st), "crop pass");
+  p->launches++;
+}
+void run_zero(gbn_plan p, float2* dst, size_t cells, cudaStream_t st) {
+  Span span(p, GBN_STAGE_ZERO, st);
+  ck(cudaMemsetAsync(dst, 0, sizeof(float2) * cells, st), "zero grid");
+}
+void run_grad(gbn_plan p, const GradArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return;
+  Span span(p, GBN_STAGE_GRAD, st);
+  ck(a.g.dim == 2 ? launch_grad2d(a, st) : launch_grad3d(a, st), "gradient kernel");
+  p->launches++;
 }
 
 PadArgs pad_args(gbn_plan p, const float2* img, const float2* smaps, int ntr, int conj_in) {
@@ -564,7 +628,7 @@ int gbn_op(gbn_plan p, const void* img, const void* smaps, void* ksp, int B, int
       // the image array is the fine grid
       for (int r0 = 0; r0 < B * C; r0 += p->ntrans) {
         int T = imin(p->ntrans, B * C - r0);
-        launch_interp_dim(interp_args(p, x + (int64_t)r0 * g.G, y + (int64_t)r0 * p->M, T,
+        run_interp(p, interp_args(p, x + (int64_t)r0 * g.G, y + (int64_t)r0 * p->M, T,
                                       scale, INTERP_STORE), st);
       }
       return;
@@ -572,10 +636,10 @@ int gbn_op(gbn_plan p, const void* img, const void* smaps, void* ksp, int B, int
     for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
       PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                      : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
-      ck(launch_pad(pa, st), "pad pass");
+      run_pad(p, pa, st);
       p->exec_fft(T, p->fine, isign, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
-      launch_interp_dim(interp_args(p, p->fine, y + row * p->M, T, scale, INTERP_STORE), st);
+      run_interp(p, interp_args(p, p->fine, y + row * p->M, T, scale, INTERP_STORE), st);
     });
   });
 }
@@ -596,20 +660,20 @@ int gbn_adj(gbn_plan p, const void* ksp, const float* density, const void* smaps
       for (int r0 = 0; r0 < B * C; r0 += p->ntrans) {
         int T = imin(p->ntrans, B * C - r0);
         float2* dst = x + (int64_t)r0 * g.G;
-        ck(cudaMemsetAsync(dst, 0, sizeof(float2) * (size_t)T * g.G, st), "zero grid");
-        launch_spread_dim(spread_args(p, y + (int64_t)r0 * p->M, density, dst, T, scale), st);
+        run_zero(p, dst, (size_t)T * g.G, st);
+        run_spread(p, spread_args(p, y + (int64_t)r0 * p->M, density, dst, T, scale), st);
       }
       return;
     }
     for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
-      ck(cudaMemsetAsync(p->fine, 0, sizeof(float2) * (size_t)T * g.G, st), "zero grid");
+      run_zero(p, p->fine, (size_t)T * g.G, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
-      launch_spread_dim(spread_args(p, y + row * p->M, density, p->fine, T, 1.0f), st);
+      run_spread(p, spread_args(p, y + row * p->M, density, p->fine, T, 1.0f), st);
       p->exec_fft(T, p->fine, isign, st);
       CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, x + (int64_t)b * g.Nimg, T,
                                   c0 > 0, scale)
                       : crop_args(p, nullptr, x + (int64_t)c0 * g.Nimg, T, 0, scale);
-      ck(launch_crop(ca, st), "crop pass");
+      run_crop(p, ca, st);
     });
   });
 }
@@ -639,20 +703,20 @@ int gbn_dc(gbn_plan p, const void* img, const void* obs, const float* density,
     for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
       PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                      : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
-      ck(launch_pad(pa, st), "pad pass");
+      run_pad(p, pa, st);
       p->exec_fft(T, p->fine, -1, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       InterpArgs ia = interp_args(p, p->fine, p->kbuf, T, scale, INTERP_RESID);
       ia.obs = yo + row * p->M;
       ia.density = density;
-      launch_interp_dim(ia, st);
-      ck(cudaMemsetAsync(p->fine, 0, sizeof(float2) * (size_t)T * g.G, st), "zero grid");
-      launch_spread_dim(spread_args(p, p->kbuf, nullptr, p->fine, T, 1.0f), st);
+      run_interp(p, ia, st);
+      run_zero(p, p->fine, (size_t)T * g.G, st);
+      run_spread(p, spread_args(p, p->kbuf, nullptr, p->fine, T, 1.0f), st);
       p->exec_fft(T, p->fine, +1, st);
       CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, gr + (int64_t)b * g.Nimg, T,
                                   c0 > 0, scale)
                       : crop_args(p, nullptr, gr + (int64_t)c0 * g.Nimg, T, 0, scale);
-      ck(launch_crop(ca, st), "crop pass");
+      run_crop(p, ca, st);
     });
   });
 }
@@ -667,9 +731,9 @@ int gbn_pipe(gbn_plan p, void* w, int iters, float scale2, gbn_stream stream) {
     float2* wv = static_cast<float2*>(w);
     const Geom& g = p->g;
     for (int it = 0; it < iters; ++it) {
-      ck(cudaMemsetAsync(p->fine, 0, sizeof(float2) * (size_t)g.G, st), "zero grid");
-      launch_spread_dim(spread_args(p, wv, nullptr, p->fine, 1, 1.0f), st);
-      launch_interp_dim(interp_args(p, p->fine, wv, 1, scale2, INTERP_PIPE), st);
+      run_zero(p, p->fine, (size_t)g.G, st);
+      run_spread(p, spread_args(p, wv, nullptr, p->fine, 1, 1.0f), st);
+      run_interp(p, interp_args(p, p->fine, wv, 1, scale2, INTERP_PIPE), st);
     }
   });
 }
@@ -683,7 +747,7 @@ static void grad_traj_common(gbn_plan p, const float2* img, const float2* s, con
   for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
     PadArgs pa = s ? pad_args(p, img + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, adjoint)
                    : pad_args(p, img + (int64_t)c0 * g.Nimg, nullptr, T, adjoint);
-    ck(launch_pad(pa, st), "pad pass");
+    run_pad(p, pa, st);
     p->exec_fft(T, p->fine, adjoint ? +1 : -1, st);
     int64_t row = s ? (int64_t)b * C + c0 : c0;
     GradArgs ga{};
@@ -695,7 +759,7 @@ static void grad_traj_common(gbn_plan p, const float2* img, const float2* s, con
     ga.ntr = T;
     ga.scale = scale;
     ga.conj_a = adjoint ? 0 : 1;
-    ck(g.dim == 2 ? launch_grad2d(ga, st) : launch_grad3d(ga, st), "gradient kernel");
+    run_grad(p, ga, st);
   });
 }
 
@@ -722,6 +786,34 @@ int gbn_grad_traj_adj(gbn_plan p, const void* dx, const void* smaps, const void*
     grad_traj_common(p, static_cast<const float2*>(dx), static_cast<const float2*>(smaps),
                      static_cast<const float2*>(y), grad, B, C, scale, 1,
                      reinterpret_cast<cudaStream_t>(stream));
+  });
+}
+
+int gbn_profile(gbn_plan p, int enable) {
+  return guarded(p, [&] {
+    for (int i = 0; i < GBN_STAGES; ++i) p->spans[i].clear();
+    p->evnext = 0;
+    p->launches = 0;
+    p->prof = enable != 0;
+  });
+}
+
+int gbn_profile_read(gbn_plan p, int stage, double* total_ms, int64_t* count) {
+  return guarded(p, [&] {
+    if (stage < -1 || stage >= GBN_STAGES) fail(GBN_ERR_ARG, "unknown stage");
+    double ms = 0.0;
+    int64_t n = 0;
+    for (int i = (stage < 0 ? 0 : stage); i < (stage < 0 ? GBN_STAGES : stage + 1); ++i) {
+      for (auto& sp : p->spans[i]) {
+        ck(cudaEventSynchronize(p->evpool[sp.second]), "cudaEventSynchronize");
+        float t = 0.f;
+        ck(cudaEventElapsedTime(&t, p->evpool[sp.first], p->evpool[sp.second]), "elapsed");
+        ms += t;
+      }
+      n += (int64_t)p->spans[i].size();
+    }
+    if (total_ms) *total_ms = ms;
+    if (count) *count = stage < 0 ? p->launches : n;
   });
 }
 

@@ -92,6 +92,39 @@ __device__ __forceinline__ int64_t tile_to_fine(const Geom& g, const int* o, int
   }
 }
 
+// Stage the padded tiles of `nc` transforms (from transform c0 on) into shared
+// memory.  Rows of the tile (all axes but the last) are spread over groups of
+// `seg` threads, seg = a power of two >= the last tile extent, so that each
+// row costs one index decomposition and the row's cells load contiguously.
+template <int DIM>
+__device__ __forceinline__ void load_tiles(float2* tile, const float2* __restrict__ fine,
+                                           const Geom& g, const int* o, int c0, int nc) {
+  const int last = DIM - 1;
+  const int pl = g.pd[last];
+  int seg = 16;
+  while (seg < pl) seg <<= 1;
+  const int rows_per_tile = DIM == 2 ? g.pd[0] : g.pd[0] * g.pd[1];
+  const int nrows = nc * rows_per_tile;
+  const int col = threadIdx.x & (seg - 1);
+  const int step = blockDim.x / seg;
+  const int mc = col < pl ? wrap_idx(o[last] + col, g.nf[last]) : 0;
+  for (int r = threadIdx.x / seg; r < nrows; r += step) {
+    if (col >= pl) continue;
+    const int cc = r / rows_per_tile;
+    const int rr = r - cc * rows_per_tile;
+    int64_t rowbase;
+    if (DIM == 2) {
+      rowbase = (int64_t)wrap_idx(o[0] + rr, g.nf[0]) * g.nf[1];
+    } else {
+      const int i1 = rr % g.pd[1];
+      const int i0 = rr / g.pd[1];
+      rowbase = ((int64_t)wrap_idx(o[0] + i0, g.nf[0]) * g.nf[1] + wrap_idx(o[1] + i1, g.nf[1])) *
+                g.nf[2];
+    }
+    tile[(int64_t)r * pl + col] = fine[(int64_t)(c0 + cc) * g.G + rowbase + mc];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Interpolation
 // ---------------------------------------------------------------------------
@@ -113,11 +146,7 @@ interp_kernel(InterpArgs a) {
 
   for (int c0 = 0; c0 < a.ntr; c0 += CG) {
     const int nc = imin(CG, a.ntr - c0);
-    for (int idx = threadIdx.x; idx < nc * T; idx += blockDim.x) {
-      int cc = idx / T;
-      int r = idx - cc * T;
-      tile[idx] = a.fine[(int64_t)(c0 + cc) * g.G + tile_to_fine<DIM>(g, o, r)];
-    }
+    load_tiles<DIM>(tile, a.fine, g, o, c0, nc);
     __syncthreads();
     for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
       const int pos = p0 + s;
@@ -210,110 +239,184 @@ GBN_UNROLL
 }
 
 // ---------------------------------------------------------------------------
-// Spreading
+// Spreading, 3D "row ownership" kernel (no shared-memory atomics).
+//
+// Shared-memory float atomics are compare-and-swap loops on this GPU, and the
+// dense k-space centre of radial trajectories makes them contend, so the 3D
+// spreader is output-driven inside each bin tile: thread t owns one row
+// (i0, i1) of the padded tile (P0 x P1 <= 16 x 16 rows, all P2 <= 16 cells
+// along axis 2) and keeps its cells in registers.  Samples of the subproblem
+// are staged in shared memory in batches of 256 (local footprint origin, the
+// axis-0/1 weights and a dense 16-cell axis-2 weight row); every thread walks
+// the batch and accumulates the samples whose footprint covers its row.
+// Rows of one warp form a 4 x 8 block, so most warps skip a sample uniformly.
+// The tile is then added to the fine grid with float2 global atomics (tiles
+// of neighbouring bins overlap by w cells).
 // ---------------------------------------------------------------------------
-template <int DIM, int W, int CG>
-__global__ void __launch_bounds__(GBN_THREADS)
-spread_kernel(SpreadArgs a) {
-  constexpr int WM = WidthTraits<W>::WM;
-  extern __shared__ float2 tile[];
+constexpr int kRowBatch = 256;
+
+template <int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS, 2)
+spread_rows3d_kernel(SpreadArgs a) {
+  constexpr int WM = W > 0 ? W : 8;
+  __shared__ int s_a0[kRowBatch], s_a1[kRowBatch];
+  __shared__ float s_w0[kRowBatch][8], s_w1[kRowBatch][8];
+  __shared__ __align__(16) float s_w2[kRowBatch][16];
+  __shared__ float2 s_c[CG][kRowBatch];
   const Geom& g = a.g;
   const int sub = blockIdx.x;
   const int b = a.s.sub_bin[sub];
   const int p0 = a.s.sub_start[sub];
   const int cnt = a.s.sub_count[sub];
   int o[3];
-  bin_origin<DIM>(g, b, o);
-  const int T = g.tile;
+  bin_origin<3>(g, b, o);
   const int w = W > 0 ? W : g.w;
-  const int WL = W > 0 ? W : w;
-  float* tf = reinterpret_cast<float*>(tile);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = 4 * (warp >> 1) + (lane >> 3);
+  const int i1 = 8 * (warp & 1) + (lane & 7);
+  const bool own = i0 < g.pd[0] && i1 < g.pd[1];
 
   for (int c0 = 0; c0 < a.ntr; c0 += CG) {
     const int nc = imin(CG, a.ntr - c0);
-    for (int idx = threadIdx.x; idx < nc * T; idx += blockDim.x) tile[idx] = make_float2(0.f, 0.f);
-    __syncthreads();
-    for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
-      const int pos = p0 + s;
-      const int j = a.s.perm[pos];
-      float dj = a.scale;
-      if (a.density) dj *= a.density[j];
-      float2 v[CG];
-GBN_UNROLL
+    float ar[CG][16], ai[CG][16];
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc)
+#pragma unroll
+      for (int z = 0; z < 16; ++z) ar[cc][z] = ai[cc][z] = 0.f;
+
+    for (int q0 = 0; q0 < cnt; q0 += kRowBatch) {
+      const int nb = imin(kRowBatch, cnt - q0);
+      if ((int)threadIdx.x < nb) {
+        const int t = threadIdx.x;
+        const int pos = p0 + q0 + t;
+        const int j = a.s.perm[pos];
+        float wt[WidthTraits<W>::WM];
+        s_a0[t] = weights_rt<W>(a.s.u[0][pos], g, wt) - o[0];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s_w0[t][k] = k < w ? wt[k] : 0.f;
+        s_a1[t] = weights_rt<W>(a.s.u[1][pos], g, wt) - o[1];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s_w1[t][k] = k < w ? wt[k] : 0.f;
+        int a2 = weights_rt<W>(a.s.u[2][pos], g, wt) - o[2];
+#pragma unroll
+        for (int z = 0; z < 16; ++z) {
+          int k = z - a2;
+          float v = 0.f;
+#pragma unroll
+          for (int kk = 0; kk < WidthTraits<W>::WM; ++kk)
+            if (kk == k && kk < w) v = wt[kk];
+          s_w2[t][z] = v;
+        }
+        float dj = a.scale;
+        if (a.density) dj *= a.density[j];
+#pragma unroll
+        for (int cc = 0; cc < CG; ++cc) {
+          float2 x = cc < nc ? a.in[(int64_t)(c0 + cc) * a.s.M + j] : make_float2(0.f, 0.f);
+          s_c[cc][t] = make_float2(x.x * dj, x.y * dj);
+        }
+      }
+      __syncthreads();
+      if (own) {
+        for (int s = 0; s < nb; ++s) {
+          const unsigned r0 = (unsigned)(i0 - s_a0[s]);
+          const unsigned r1 = (unsigned)(i1 - s_a1[s]);
+          if (r0 < (unsigned)w && r1 < (unsigned)w) {
+            const float k = s_w0[s][r0] * s_w1[s][r1];
+            float wz[16];
+            const float4* w4 = reinterpret_cast<const float4*>(s_w2[s]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float4 v = w4[q];
+              wz[4 * q] = v.x;
+              wz[4 * q + 1] = v.y;
+              wz[4 * q + 2] = v.z;
+              wz[4 * q + 3] = v.w;
+            }
+#pragma unroll
+            for (int cc = 0; cc < CG; ++cc) {
+              const float2 c = s_c[cc][s];
+              const float vr = k * c.x, vi = k * c.y;
+#pragma unroll
+              for (int z = 0; z < 16; ++z) {
+                ar[cc][z] = fmaf(vr, wz[z], ar[cc][z]);
+                ai[cc][z] = fmaf(vi, wz[z], ai[cc][z]);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (own) {
+      const int m0 = wrap_idx(o[0] + i0, g.nf[0]);
+      const int m1 = wrap_idx(o[1] + i1, g.nf[1]);
+      const int64_t rowbase = ((int64_t)m0 * g.nf[1] + m1) * g.nf[2];
+#pragma unroll
       for (int cc = 0; cc < CG; ++cc) {
         if (cc < nc) {
-          float2 x = a.in[(int64_t)(c0 + cc) * a.s.M + j];
-          v[cc] = make_float2(x.x * dj, x.y * dj);
+          float2* dst = a.fine + (int64_t)(c0 + cc) * g.G + rowbase;
+#pragma unroll
+          for (int z = 0; z < 16; ++z) {
+            if (z < g.pd[2] && (ar[cc][z] != 0.f || ai[cc][z] != 0.f))
+              atomicAdd(dst + wrap_idx(o[2] + z, g.nf[2]), make_float2(ar[cc][z], ai[cc][z]));
+          }
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Spreading, sample-driven kernel with global vector atomics (2D, and any
+// width the row kernel does not cover).  Threads take consecutive sorted
+// samples, so the float2 reductions of a warp land on nearby cells of the
+// same L2 sectors.
+// ---------------------------------------------------------------------------
+template <int DIM, int W>
+__global__ void __launch_bounds__(GBN_THREADS)
+spread_gm_kernel(SpreadArgs a) {
+  constexpr int WM = WidthTraits<W>::WM;
+  const Geom& g = a.g;
+  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= a.s.M) return;
+  const int w = W > 0 ? W : g.w;
+  const int WL = W > 0 ? W : w;
+  const int j = a.s.perm[pos];
+  float w0[WM], w1[WM], w2[WM];
+  int m0[WM], m1[WM], m2[WM];
+  int i0 = weights_rt<W>(a.s.u[0][pos], g, w0);
+  int i1 = weights_rt<W>(a.s.u[1][pos], g, w1);
+  int i2 = 0;
+  if (DIM == 3) i2 = weights_rt<W>(a.s.u[2][pos], g, w2);
+GBN_UNROLL
+  for (int t = 0; t < WL; ++t) {
+    m0[t] = wrap_idx(i0 + t, g.nf[0]);
+    m1[t] = wrap_idx(i1 + t, g.nf[1]);
+    if (DIM == 3) m2[t] = wrap_idx(i2 + t, g.nf[2]);
+  }
+  float dj = a.scale;
+  if (a.density) dj *= a.density[j];
+  for (int c = 0; c < a.ntr; ++c) {
+    float2 x = a.in[(int64_t)c * a.s.M + j];
+    const float vr = x.x * dj, vi = x.y * dj;
+    float2* base = a.fine + (int64_t)c * g.G;
+GBN_UNROLL
+    for (int t0 = 0; t0 < WL; ++t0) {
+GBN_UNROLL
+      for (int t1 = 0; t1 < WL; ++t1) {
+        const float k = w0[t0] * w1[t1];
+        const int64_t r = (int64_t)m0[t0] * g.nf[1] + m1[t1];
+        if (DIM == 2) {
+          atomicAdd(base + r, make_float2(k * vr, k * vi));
         } else {
-          v[cc] = make_float2(0.f, 0.f);
-        }
-      }
-      float w0[WM], w1[WM], w2[WM];
-      int l0 = weights_rt<W>(a.s.u[0][pos], g, w0) - o[0];
-      int l1 = weights_rt<W>(a.s.u[1][pos], g, w1) - o[1];
-      int l2 = 0;
-      if (DIM == 3) l2 = weights_rt<W>(a.s.u[2][pos], g, w2) - o[2];
-      if (DIM == 2) {
 GBN_UNROLL
-        for (int t0 = 0; t0 < WL; ++t0) {
-          {
-            const int rbase = (l0 + t0) * g.pd[1] + l1;
-GBN_UNROLL
-            for (int t1 = 0; t1 < WL; ++t1) {
-              {
-                const float k = w0[t0] * w1[t1];
-GBN_UNROLL
-                for (int cc = 0; cc < CG; ++cc) {
-                  if (cc < nc) {
-                    float* p = tf + 2 * (cc * T + rbase + t1);
-                    atomicAdd(p, k * v[cc].x);
-                    atomicAdd(p + 1, k * v[cc].y);
-                  }
-                }
-              }
-            }
-          }
-        }
-      } else {
-GBN_UNROLL
-        for (int t0 = 0; t0 < WL; ++t0) {
-          {
-GBN_UNROLL
-            for (int t1 = 0; t1 < WL; ++t1) {
-              {
-                const float wy = w0[t0] * w1[t1];
-                const int rbase = ((l0 + t0) * g.pd[1] + (l1 + t1)) * g.pd[2] + l2;
-GBN_UNROLL
-                for (int t2 = 0; t2 < WL; ++t2) {
-                  {
-                    const float k = wy * w2[t2];
-GBN_UNROLL
-                    for (int cc = 0; cc < CG; ++cc) {
-                      if (cc < nc) {
-                        float* p = tf + 2 * (cc * T + rbase + t2);
-                        atomicAdd(p, k * v[cc].x);
-                        atomicAdd(p + 1, k * v[cc].y);
-                      }
-                    }
-                  }
-                }
-              }
-            }
+          for (int t2 = 0; t2 < WL; ++t2) {
+            const float kk = k * w2[t2];
+            atomicAdd(base + r * g.nf[2] + m2[t2], make_float2(kk * vr, kk * vi));
           }
         }
       }
     }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < nc * T; idx += blockDim.x) {
-      float2 v = tile[idx];
-      if (v.x != 0.f || v.y != 0.f) {
-        int cc = idx / T;
-        int r = idx - cc * T;
-        float2* dst = a.fine + (int64_t)(c0 + cc) * g.G + tile_to_fine<DIM>(g, o, r);
-        atomicAdd(dst, v);
-      }
-    }
-    __syncthreads();
   }
 }
 
@@ -338,8 +441,7 @@ grad_kernel(GradArgs a, int conj_a) {
   const int WL = W > 0 ? W : w;
 
   for (int c = 0; c < a.ntr; ++c) {
-    for (int idx = threadIdx.x; idx < T; idx += blockDim.x)
-      tile[idx] = a.fine[(int64_t)c * g.G + tile_to_fine<DIM>(g, o, idx)];
+    load_tiles<DIM>(tile, a.fine, g, o, c, 1);
     __syncthreads();
     for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
       const int pos = p0 + s;
@@ -412,14 +514,18 @@ cudaError_t launch_interp_t(const InterpArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int DIM, int W, int CG>
-cudaError_t launch_spread_t(const SpreadArgs& a, cudaStream_t st) {
+template <int W, int CG>
+cudaError_t launch_spread_rows_t(const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return cudaSuccess;
-  size_t smem = (size_t)CG * a.g.tile * sizeof(float2);
-  auto k = spread_kernel<DIM, W, CG>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k<<<a.s.nsub, GBN_THREADS, smem, st>>>(a);
+  spread_rows3d_kernel<W, CG><<<a.s.nsub, GBN_THREADS, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int DIM, int W>
+cudaError_t launch_spread_gm_t(const SpreadArgs& a, cudaStream_t st) {
+  if (a.s.M == 0) return cudaSuccess;
+  unsigned blocks = (unsigned)((a.s.M + GBN_THREADS - 1) / GBN_THREADS);
+  spread_gm_kernel<DIM, W><<<blocks, GBN_THREADS, 0, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -442,14 +548,6 @@ cudaError_t dispatch_interp_w(const InterpArgs& a, cudaStream_t st) {
   return launch_interp_t<DIM, 0, CG>(a, st);
 }
 
-template <int DIM, int CG>
-cudaError_t dispatch_spread_w(const SpreadArgs& a, cudaStream_t st) {
-  // w = 7 is the width of mri-nufft's default eps = 1e-6 at upsampfac 2;
-  // every other width runs the runtime-width kernel.
-  if (a.g.w == 7) return launch_spread_t<DIM, 7, CG>(a, st);
-  return launch_spread_t<DIM, 0, CG>(a, st);
-}
-
 template <int DIM>
 cudaError_t dispatch_interp(const InterpArgs& a, cudaStream_t st) {
   int cg = a.mode == INTERP_PIPE ? 1 : coils_per_pass(a.g, a.ntr);
@@ -457,11 +555,20 @@ cudaError_t dispatch_interp(const InterpArgs& a, cudaStream_t st) {
   return dispatch_interp_w<DIM, 1>(a, st);
 }
 
+// 3D tiles up to 16 x 16 x 16 cells use the row kernel (two coils per pass);
+// 2D, and wider kernels, use the sample-driven global-atomic kernel.
+inline bool rows_fit(const Geom& g) {
+  return g.dim == 3 && g.w <= 8 && g.pd[0] <= 16 && g.pd[1] <= 16 && g.pd[2] <= 16;
+}
+
 template <int DIM>
 cudaError_t dispatch_spread(const SpreadArgs& a, cudaStream_t st) {
-  int cg = coils_per_pass(a.g, a.ntr);
-  if (cg >= 2) return dispatch_spread_w<DIM, 4>(a, st);
-  return dispatch_spread_w<DIM, 1>(a, st);
+  if (DIM == 3 && rows_fit(a.g)) {
+    if (a.g.w == 7) return a.ntr > 1 ? launch_spread_rows_t<7, 2>(a, st) : launch_spread_rows_t<7, 1>(a, st);
+    return a.ntr > 1 ? launch_spread_rows_t<0, 2>(a, st) : launch_spread_rows_t<0, 1>(a, st);
+  }
+  if (a.g.w == 7) return launch_spread_gm_t<DIM, 7>(a, st);
+  return launch_spread_gm_t<DIM, 0>(a, st);
 }
 
 template <int DIM>

@@ -81,6 +81,21 @@ class NufftPlan:
         _lib.check(self.lib.gbn_plan_device_bytes(self._h, ctypes.byref(b)), "gbn_plan_device_bytes")
         return b.value
 
+    # ------------------------------------------------------------- profiling
+    def profile(self, enable: bool = True):
+        """Start (clear) or stop per-stage CUDA-event timing."""
+        _lib.check(self.lib.gbn_profile(self._h, int(enable)), "gbn_profile")
+
+    def profile_read(self, stage: str | None = None):
+        """(device ms, launches) of a stage, or of all stages and the number of
+        this library's kernel launches when ``stage`` is None."""
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        idx = -1 if stage is None else _lib.STAGES[stage]
+        _lib.check(self.lib.gbn_profile_read(self._h, idx, ctypes.byref(ms), ctypes.byref(n)),
+                   "gbn_profile_read")
+        return ms.value, n.value
+
     # ---------------------------------------------------------------- points
     def setpts(self, samples: torch.Tensor):
         """Set the (M, d) float32 CUDA sample coordinates in radians."""
