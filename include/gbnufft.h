@@ -182,6 +182,29 @@ int gbn_norm2_f64(const void* x, int64_t n, double* out, gbn_stream stream);
 int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* out,
                  gbn_stream stream);
 
+/*
+ * Pipe density iterations that allocate nothing.  No counterpart in the
+ * reference: it is the gbn_pipe iteration for callers that cannot allocate
+ * device memory at the time they need it (a process whose device memory is
+ * held by a framework's pool, or a real-time reconstruction service that
+ * forbids allocation after start-up).  It needs no plan: the image-size grid
+ * lives in a fixed device array of GBN_STATIC_GRID_CELLS complex64 cells
+ * (16 MiB, held on every GPU that loads the library until exit), and the
+ * samples are used unsorted.  Same arguments and result as
+ * gbn_plan_create(dim, n_modes, osf, eps, 1, 1, dev) + gbn_setpts + gbn_pipe:
+ * `iters` times w <- w / |scale2 * interp(spread(w))| on the n_modes grid,
+ * w complex64 of length M, coordinates float32 radians, on the current
+ * device.  Grids of more than GBN_STATIC_GRID_CELLS cells are rejected
+ * (GBN_ERR_ARG).  The first call on a device looks the array up with
+ * cudaGetSymbolAddress and should come before any stream capture.  Every
+ * call shares the array (each iteration clears it first): calls whose work
+ * overlaps on the GPU race and must be serialised by the caller.
+ */
+#define GBN_STATIC_GRID_CELLS (1 << 21)
+int gbn_pipe_static(int dim, const int64_t* n_modes, double osf, double eps, int64_t M,
+                    const float* k0, const float* k1, const float* k2, void* w, int iters,
+                    float scale2, gbn_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -174,6 +174,8 @@ std::vector<float> deconv_factors(int N, int64_t nf, int w, double beta) {
 
 }  // namespace
 
+void gbn::set_last_error(const char* msg) { g_err = msg; }
+
 struct gbn_plan_s {
   Geom g{};
   int ntrans = 1;

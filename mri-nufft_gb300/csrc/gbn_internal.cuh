@@ -134,6 +134,9 @@ __device__ __forceinline__ int cell_of(float u, int nf) {
   return f > nf - 1 ? nf - 1 : f;
 }
 
+// Sets the message returned by gbn_last_error() on the calling thread.
+void set_last_error(const char* msg);
+
 // Launchers implemented in the per-dimension translation units.
 cudaError_t launch_interp2d(const InterpArgs& a, cudaStream_t st);
 cudaError_t launch_interp3d(const InterpArgs& a, cudaStream_t st);
