@@ -12,6 +12,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
@@ -252,6 +253,7 @@ struct gbn_plan_s {
     s.sub_start = sb.sub_start;
     s.sub_count = sb.sub_count;
     s.nsub = nsub;
+    s.maxsub = maxsub;
     return s;
   }
 
@@ -478,8 +480,23 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
     g.inv_halfw = 2.0f / w;
     g.G = 1;
     g.Nimg = 1;
-    const int binsz2[2] = {32, 32};
-    const int binsz3[3] = {8, 8, 8};
+    int binsz2[2] = {32, 32};
+    int binsz3[3] = {8, 8, 8};
+    // tuning overrides: GBN_BINS2="b0,b1", GBN_BINS3="b0,b1,b2", GBN_INTERP_CG=1|2|4
+    if (const char* e = std::getenv(dim == 2 ? "GBN_BINS2" : "GBN_BINS3")) {
+      int v[3] = {0, 0, 0};
+      if (std::sscanf(e, "%d,%d,%d", &v[0], &v[1], &v[2]) >= dim)
+        for (int d = 0; d < dim; ++d)
+          if (v[d] >= 1 && v[d] <= 64) (dim == 2 ? binsz2[d] : binsz3[d]) = v[d];
+    }
+    if (const char* e = std::getenv("GBN_INTERP_CG")) g.interp_cg = std::atoi(e);
+    if (const char* e = std::getenv("GBN_INTERP"))
+      g.method_interp = std::strcmp(e, "gm") == 0   ? 1
+                        : std::strcmp(e, "db") == 0 ? 3
+                        : std::strcmp(e, "wc") == 0 ? 4
+                        : std::strcmp(e, "twc") == 0 ? 5
+                                                     : 0;
+    if (const char* e = std::getenv("GBN_SPREAD")) g.method_spread = std::strcmp(e, "gm") == 0;
     for (int d = 0; d < 3; ++d) {
       if (d < dim) {
         int64_t N = n_modes[d];
@@ -580,8 +597,13 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
     if (M > 0 && (!k0 || !k1 || (p->g.dim == 3 && !k2))) fail(GBN_ERR_ARG, "null coordinates");
     // subproblem size: aim at >= 4 subproblems per SM, 32..1024 samples
     int64_t target = M / (4 * (int64_t)p->nsm);
+    int cap = 512;
+    if (const char* e = std::getenv("GBN_MAXSUB")) {
+      int v = std::atoi(e);
+      if (v >= 32 && v <= 65536) cap = v;
+    }
     int maxsub = 32;
-    while (maxsub < target && maxsub < 1024) maxsub <<= 1;
+    while (maxsub < target && maxsub < cap) maxsub <<= 1;
     int64_t subcap = M / maxsub + (M < p->nbins ? M : p->nbins) + 1;
     if (M > p->Mcap || subcap > p->subcap) {
       // free the previous point buffers before the new ones (bytes tally)

@@ -36,6 +36,9 @@ struct Geom {
   int64_t G;     // fine cells per transform
   int64_t Nimg;  // image pixels per transform
   int tile;      // padded tile cells = prod(pd)
+  int interp_cg; // coils per interp tile pass (0: automatic)
+  int method_interp;  // 0: tiles, 1: direct from the fine grid, 3: double-buffered tiles
+  int method_spread;  // 0: automatic, 1: global atomics
 };
 
 // Work table of one sorted trajectory.
@@ -47,6 +50,7 @@ struct Sorted {
   const int* sub_start;   // subproblem -> first sorted position
   const int* sub_count;   // subproblem -> number of samples
   int nsub;
+  int maxsub;             // largest subproblem
 };
 
 // Interp epilogues.
@@ -148,11 +152,13 @@ cudaError_t launch_grad3d(const GradArgs& a, cudaStream_t st);
 // Shared-memory budget for the tiles of one CTA.
 constexpr int kTileSmemBudget = 112 * 1024;
 
-// coils per tile pass: 4 when four tiles fit the budget and there is more
-// than one transform, else 1.
+// coils per interp tile pass: 1 (or the plan's override), halved until the
+// tiles fit the shared-memory budget and do not exceed the transform count.
 inline int coils_per_pass(const Geom& g, int ntr) {
   size_t t = (size_t)g.tile * sizeof(float2);
-  return (ntr > 1 && 4 * t <= (size_t)kTileSmemBudget) ? 4 : 1;
+  int cg = g.interp_cg > 0 ? g.interp_cg : 1;
+  while (cg > 1 && (cg > ntr || (size_t)cg * t > (size_t)kTileSmemBudget)) cg >>= 1;
+  return cg;
 }
 
 }  // namespace gbn

@@ -239,6 +239,445 @@ GBN_UNROLL
 }
 
 // ---------------------------------------------------------------------------
+// Interpolation with double-buffered tiles: each thread keeps the weights of
+// its (at most S) samples in registers for all transforms, and the tile of
+// transform c+1 streams into shared memory with cp.async while transform c
+// is interpolated.  maxsub <= S * GBN_THREADS.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async8(float2* dst, const float2* src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int DIM>
+__device__ __forceinline__ void load_tile_async(float2* tile, const float2* __restrict__ fine,
+                                                const Geom& g, const int* o) {
+  const int last = DIM - 1;
+  const int pl = g.pd[last];
+  int seg = 16;
+  while (seg < pl) seg <<= 1;
+  const int nrows = DIM == 2 ? g.pd[0] : g.pd[0] * g.pd[1];
+  const int col = threadIdx.x & (seg - 1);
+  if (col >= pl) return;
+  const int step = blockDim.x / seg;
+  const int mc = wrap_idx(o[last] + col, g.nf[last]);
+  for (int r = threadIdx.x / seg; r < nrows; r += step) {
+    int64_t rowbase;
+    if (DIM == 2) {
+      rowbase = (int64_t)wrap_idx(o[0] + r, g.nf[0]) * g.nf[1];
+    } else {
+      const int i1 = r % g.pd[1];
+      const int i0 = r / g.pd[1];
+      rowbase = ((int64_t)wrap_idx(o[0] + i0, g.nf[0]) * g.nf[1] + wrap_idx(o[1] + i1, g.nf[1])) *
+                g.nf[2];
+    }
+    cp_async8(tile + r * pl + col, fine + rowbase + mc);
+  }
+}
+
+template <int DIM, int W, int S>
+__global__ void __launch_bounds__(GBN_THREADS)
+interp_db_kernel(InterpArgs a) {
+  extern __shared__ float2 tiles[];
+  const Geom& g = a.g;
+  const int sub = blockIdx.x;
+  const int b = a.s.sub_bin[sub];
+  const int p0 = a.s.sub_start[sub];
+  const int cnt = a.s.sub_count[sub];
+  int o[3];
+  bin_origin<DIM>(g, b, o);
+  const int T = g.tile;
+  float w0[S][W], w1[S][W], w2[S][W];
+  int l0[S], l1[S], l2[S], jj[S];
+#pragma unroll
+  for (int q = 0; q < S; ++q) {
+    const int s = threadIdx.x + q * GBN_THREADS;
+    jj[q] = -1;
+    l0[q] = l1[q] = l2[q] = 0;
+    if (s < cnt) {
+      const int pos = p0 + s;
+      jj[q] = a.s.perm[pos];
+      l0[q] = weights_rt<W>(a.s.u[0][pos], g, w0[q]) - o[0];
+      l1[q] = weights_rt<W>(a.s.u[1][pos], g, w1[q]) - o[1];
+      if (DIM == 3) l2[q] = weights_rt<W>(a.s.u[2][pos], g, w2[q]) - o[2];
+    }
+  }
+  load_tile_async<DIM>(tiles, a.fine, g, o);
+  cp_async_commit();
+  for (int c = 0; c < a.ntr; ++c) {
+    if (c + 1 < a.ntr) {
+      load_tile_async<DIM>(tiles + ((c + 1) & 1) * T, a.fine + (int64_t)(c + 1) * g.G, g, o);
+      cp_async_commit();
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const float2* tile = tiles + (c & 1) * T;
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+      if (jj[q] < 0) continue;
+      float ar = 0.f, ai = 0.f;
+      if (DIM == 2) {
+#pragma unroll
+        for (int t0 = 0; t0 < W; ++t0) {
+          const float2* row = tile + (l0[q] + t0) * g.pd[1] + l1[q];
+          float sr = 0.f, si = 0.f;
+#pragma unroll
+          for (int t1 = 0; t1 < W; ++t1) {
+            const float2 v = row[t1];
+            sr = fmaf(w1[q][t1], v.x, sr);
+            si = fmaf(w1[q][t1], v.y, si);
+          }
+          ar = fmaf(w0[q][t0], sr, ar);
+          ai = fmaf(w0[q][t0], si, ai);
+        }
+      } else {
+#pragma unroll
+        for (int t0 = 0; t0 < W; ++t0) {
+#pragma unroll
+          for (int t1 = 0; t1 < W; ++t1) {
+            const float2* row = tile + ((l0[q] + t0) * g.pd[1] + (l1[q] + t1)) * g.pd[2] + l2[q];
+            float sr = 0.f, si = 0.f;
+#pragma unroll
+            for (int t2 = 0; t2 < W; ++t2) {
+              const float2 v = row[t2];
+              sr = fmaf(w2[q][t2], v.x, sr);
+              si = fmaf(w2[q][t2], v.y, si);
+            }
+            const float k = w0[q][t0] * w1[q][t1];
+            ar = fmaf(k, sr, ar);
+            ai = fmaf(k, si, ai);
+          }
+        }
+      }
+      const int j = jj[q];
+      if (a.mode == INTERP_PIPE) {
+        float2 cur = a.out[j];
+        float mag = a.scale * sqrtf(ar * ar + ai * ai);
+        a.out[j] = make_float2(cur.x / mag, cur.y / mag);
+      } else {
+        const int64_t oi = (int64_t)c * a.s.M + j;
+        float2 r = make_float2(a.scale * ar, a.scale * ai);
+        if (a.mode == INTERP_RESID) {
+          float2 ob = a.obs[oi];
+          r.x -= ob.x;
+          r.y -= ob.y;
+          if (a.density) {
+            float dj = a.density[j];
+            r.x *= dj;
+            r.y *= dj;
+          }
+        }
+        a.out[oi] = r;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interpolation straight from the fine grid (no shared-memory tile): thread
+// per sorted sample, weights evaluated once and reused by every transform,
+// footprint cells read through L1 (consecutive sorted samples of a warp read
+// overlapping cells).
+// ---------------------------------------------------------------------------
+template <int DIM, int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS, 4)
+interp_gm_kernel(InterpArgs a) {
+  constexpr int WM = WidthTraits<W>::WM;
+  const Geom& g = a.g;
+  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= a.s.M) return;
+  const int w = W > 0 ? W : g.w;
+  const int WL = W > 0 ? W : w;
+  const int j = a.s.perm[pos];
+  float w0[WM], w1[WM], w2[WM];
+  int m0[WM], m1[WM], m2[WM];
+  int i0 = weights_rt<W>(a.s.u[0][pos], g, w0);
+  int i1 = weights_rt<W>(a.s.u[1][pos], g, w1);
+  int i2 = 0;
+  if (DIM == 3) i2 = weights_rt<W>(a.s.u[2][pos], g, w2);
+GBN_UNROLL
+  for (int t = 0; t < WL; ++t) {
+    m0[t] = wrap_idx(i0 + t, g.nf[0]);
+    m1[t] = wrap_idx(i1 + t, g.nf[1]);
+    if (DIM == 3) m2[t] = wrap_idx(i2 + t, g.nf[2]);
+  }
+  for (int c0 = 0; c0 < a.ntr; c0 += CG) {
+    const int nc = imin(CG, a.ntr - c0);
+    float ar[CG], ai[CG];
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc) ar[cc] = ai[cc] = 0.f;
+#pragma unroll 1
+    for (int t0 = 0; t0 < WL; ++t0) {
+#pragma unroll 1
+      for (int t1 = 0; t1 < WL; ++t1) {
+        const int64_t r = (int64_t)m0[t0] * g.nf[1] + m1[t1];
+        const float k = w0[t0] * w1[t1];
+#pragma unroll
+        for (int cc = 0; cc < CG; ++cc) {
+          if (cc < nc) {
+            const float2* base = a.fine + (int64_t)(c0 + cc) * g.G;
+            float sr = 0.f, si = 0.f;
+            if (DIM == 2) {
+              const float2 v = __ldg(base + r);
+              sr = v.x;
+              si = v.y;
+            } else {
+              const float2* row = base + r * g.nf[2];
+GBN_UNROLL
+              for (int t2 = 0; t2 < WL; ++t2) {
+                const float2 v = __ldg(row + m2[t2]);
+                sr = fmaf(w2[t2], v.x, sr);
+                si = fmaf(w2[t2], v.y, si);
+              }
+            }
+            ar[cc] = fmaf(k, sr, ar[cc]);
+            ai[cc] = fmaf(k, si, ai[cc]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc) {
+      if (cc >= nc) continue;
+      if (a.mode == INTERP_PIPE) {
+        float2 cur = a.out[j];
+        float mag = a.scale * sqrtf(ar[cc] * ar[cc] + ai[cc] * ai[cc]);
+        a.out[j] = make_float2(cur.x / mag, cur.y / mag);
+      } else {
+        const int64_t oi = (int64_t)(c0 + cc) * a.s.M + j;
+        float2 r = make_float2(a.scale * ar[cc], a.scale * ai[cc]);
+        if (a.mode == INTERP_RESID) {
+          float2 ob = a.obs[oi];
+          r.x -= ob.x;
+          r.y -= ob.y;
+          if (a.density) {
+            float dj = a.density[j];
+            r.x *= dj;
+            r.y *= dj;
+          }
+        }
+        a.out[oi] = r;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative interpolation straight from the fine grid (w = 7).
+// Eight lanes serve one sample: lane l reads footprint cells along the last
+// axis at offset l (7 contiguous float2 per row, i.e. 56 coalesced bytes per
+// sample), so one warp instruction loads the rows of four samples in a few
+// sectors; partial sums are combined with three butterfly shuffles.  The
+// kernel weights of a sample stay in registers for every transform.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(GBN_THREADS, 4)
+interp_wc_kernel(InterpArgs a) {
+  constexpr int W = 7;
+  const Geom& g = a.g;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane >> 3, l = lane & 7;
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t pos = warp_id * 4 + sub;
+  const bool valid = pos < a.s.M;
+  const bool act = valid && l < W;
+  float w0[W], w1[W];
+  float wl = 0.f;
+  int rb[W];  // row index m0 * nf1 (< 2^31: fine grids are capped at 2^31 cells)
+  int m1[W];
+  int ml = 0, j = 0;
+  if (valid) {
+    j = a.s.perm[pos];
+    const float u0 = a.s.u[0][pos], u1 = a.s.u[1][pos];
+    const int i0 = weights_rt<W>(u0, g, w0);
+    if (DIM == 2) {
+      const float s1 = u1 - g.halfw;
+      const int i1 = (int)ceilf(s1);
+      wl = l < W ? es_eval((float)(i1 + l) - u1, g.beta, g.inv_halfw) : 0.f;
+      ml = wrap_idx(i1 + l, g.nf[1]);
+#pragma unroll
+      for (int t = 0; t < W; ++t) rb[t] = wrap_idx(i0 + t, g.nf[0]) * g.nf[1];
+    } else {
+      const int i1 = weights_rt<W>(u1, g, w1);
+      const float u2 = a.s.u[2][pos];
+      const int i2 = (int)ceilf(u2 - g.halfw);
+      wl = l < W ? es_eval((float)(i2 + l) - u2, g.beta, g.inv_halfw) : 0.f;
+      ml = wrap_idx(i2 + l, g.nf[2]);
+#pragma unroll
+      for (int t = 0; t < W; ++t) {
+        rb[t] = wrap_idx(i0 + t, g.nf[0]) * g.nf[1];
+        m1[t] = wrap_idx(i1 + t, g.nf[1]);
+      }
+    }
+  }
+  for (int c = 0; c < a.ntr; ++c) {
+    const float2* base = a.fine + (int64_t)c * g.G;
+    float ar = 0.f, ai = 0.f;
+    if (act) {
+      if (DIM == 2) {
+#pragma unroll
+        for (int t0 = 0; t0 < W; ++t0) {
+          const float2 v = __ldg(base + rb[t0] + ml);
+          ar = fmaf(w0[t0], v.x, ar);
+          ai = fmaf(w0[t0], v.y, ai);
+        }
+        ar *= wl;
+        ai *= wl;
+      } else {
+#pragma unroll
+        for (int t0 = 0; t0 < W; ++t0) {
+          float sr = 0.f, si = 0.f;
+#pragma unroll
+          for (int t1 = 0; t1 < W; ++t1) {
+            const float2 v = __ldg(base + (int64_t)(rb[t0] + m1[t1]) * g.nf[2] + ml);
+            sr = fmaf(w1[t1], v.x, sr);
+            si = fmaf(w1[t1], v.y, si);
+          }
+          ar = fmaf(w0[t0], sr, ar);
+          ai = fmaf(w0[t0], si, ai);
+        }
+        ar *= wl;
+        ai *= wl;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      ar += __shfl_xor_sync(0xffffffffu, ar, o);
+      ai += __shfl_xor_sync(0xffffffffu, ai, o);
+    }
+    if (valid && l == 0) {
+      if (a.mode == INTERP_PIPE) {
+        float2 cur = a.out[j];
+        float mag = a.scale * sqrtf(ar * ar + ai * ai);
+        a.out[j] = make_float2(cur.x / mag, cur.y / mag);
+      } else {
+        const int64_t oi = (int64_t)c * a.s.M + j;
+        float2 r = make_float2(a.scale * ar, a.scale * ai);
+        if (a.mode == INTERP_RESID) {
+          float2 ob = a.obs[oi];
+          r.x -= ob.x;
+          r.y -= ob.y;
+          if (a.density) {
+            float dj = a.density[j];
+            r.x *= dj;
+            r.y *= dj;
+          }
+        }
+        a.out[oi] = r;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tile + warp-cooperative interpolation (3D, w = 7).  Per subproblem the
+// samples' local footprint origins and weights are computed once into shared
+// memory; then for each transform the padded tile is staged in shared memory
+// and every warp serves groups of four samples with eight lanes each (lane l
+// reads the 7-cell rows at offset l: conflict-free, 56 contiguous bytes per
+// sample), reducing with butterfly shuffles.  Sparse bins keep all warps
+// busy because work is spread by sample groups, not by threads.
+// ---------------------------------------------------------------------------
+constexpr int kTwcMaxSub = 256;
+
+static __global__ void __launch_bounds__(GBN_THREADS)
+interp_twc3d_kernel(InterpArgs a) {
+  constexpr int W = 7;
+  extern __shared__ float2 tile[];
+  __shared__ float s_w0[kTwcMaxSub][8], s_w1[kTwcMaxSub][8], s_w2[kTwcMaxSub][8];
+  __shared__ int s_off[kTwcMaxSub], s_j[kTwcMaxSub];
+  const Geom& g = a.g;
+  const int sub = blockIdx.x;
+  const int b = a.s.sub_bin[sub];
+  const int p0 = a.s.sub_start[sub];
+  const int cnt = a.s.sub_count[sub];
+  int o[3];
+  bin_origin<3>(g, b, o);
+  for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
+    const int pos = p0 + s;
+    float wt[W];
+    const int l0 = weights_rt<W>(a.s.u[0][pos], g, wt) - o[0];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) s_w0[s][t] = t < W ? wt[t] : 0.f;
+    const int l1 = weights_rt<W>(a.s.u[1][pos], g, wt) - o[1];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) s_w1[s][t] = t < W ? wt[t] : 0.f;
+    const int l2 = weights_rt<W>(a.s.u[2][pos], g, wt) - o[2];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) s_w2[s][t] = t < W ? wt[t] : 0.f;
+    s_off[s] = (l0 * g.pd[1] + l1) * g.pd[2] + l2;
+    s_j[s] = a.s.perm[pos];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int q = lane >> 3, l = lane & 7;
+  const int ngroups = (cnt + 3) >> 2;
+  const int pd12 = g.pd[1] * g.pd[2];
+  for (int c = 0; c < a.ntr; ++c) {
+    __syncthreads();  // previous tile consumed, sample table written
+    load_tiles<3>(tile, a.fine, g, o, c, 1);
+    __syncthreads();
+    for (int gi = warp; gi < ngroups; gi += (GBN_THREADS / 32)) {
+      const int s = gi * 4 + q;
+      const bool valid = s < cnt;
+      float ar = 0.f, ai = 0.f;
+      if (valid && l < W) {
+        const float2* t = tile + s_off[s] + l;
+        const float wl = s_w2[s][l];
+#pragma unroll
+        for (int t0 = 0; t0 < W; ++t0) {
+          float sr = 0.f, si = 0.f;
+#pragma unroll
+          for (int t1 = 0; t1 < W; ++t1) {
+            const float2 v = t[t0 * pd12 + t1 * g.pd[2]];
+            const float w1 = s_w1[s][t1];
+            sr = fmaf(w1, v.x, sr);
+            si = fmaf(w1, v.y, si);
+          }
+          const float w0 = s_w0[s][t0];
+          ar = fmaf(w0, sr, ar);
+          ai = fmaf(w0, si, ai);
+        }
+        ar *= wl;
+        ai *= wl;
+      }
+#pragma unroll
+      for (int m = 1; m < 8; m <<= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, m);
+        ai += __shfl_xor_sync(0xffffffffu, ai, m);
+      }
+      if (valid && l == 0) {
+        const int j = s_j[s];
+        if (a.mode == INTERP_PIPE) {
+          float2 cur = a.out[j];
+          float mag = a.scale * sqrtf(ar * ar + ai * ai);
+          a.out[j] = make_float2(cur.x / mag, cur.y / mag);
+        } else {
+          const int64_t oi = (int64_t)c * a.s.M + j;
+          float2 r = make_float2(a.scale * ar, a.scale * ai);
+          if (a.mode == INTERP_RESID) {
+            float2 ob = a.obs[oi];
+            r.x -= ob.x;
+            r.y -= ob.y;
+            if (a.density) {
+              float dj = a.density[j];
+              r.x *= dj;
+              r.y *= dj;
+            }
+          }
+          a.out[oi] = r;
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Spreading, 3D "row ownership" kernel (no shared-memory atomics).
 //
 // Shared-memory float atomics are compare-and-swap loops on this GPU, and the
@@ -249,7 +688,7 @@ GBN_UNROLL
 // are staged in shared memory in batches of 256 (local footprint origin, the
 // axis-0/1 weights and a dense 16-cell axis-2 weight row); every thread walks
 // the batch and accumulates the samples whose footprint covers its row.
-// Rows of one warp form a 4 x 8 block, so most warps skip a sample uniformly.
+// Each warp owns two rows of i0, so most warps skip a sample uniformly.
 // The tile is then added to the fine grid with float2 global atomics (tiles
 // of neighbouring bins overlap by w cells).
 // ---------------------------------------------------------------------------
@@ -271,9 +710,11 @@ spread_rows3d_kernel(SpreadArgs a) {
   int o[3];
   bin_origin<3>(g, b, o);
   const int w = W > 0 ? W : g.w;
+  // warp w owns rows i0 = 2w, 2w+1 (16 lanes each along i1): a footprint of
+  // 7 consecutive i0 rows touches 4 warps
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i0 = 4 * (warp >> 1) + (lane >> 3);
-  const int i1 = 8 * (warp & 1) + (lane & 7);
+  const int i0 = 2 * warp + (lane >> 4);
+  const int i1 = lane & 15;
   const bool own = i0 < g.pd[0] && i1 < g.pd[1];
 
   for (int c0 = 0; c0 < a.ntr; c0 += CG) {
@@ -548,10 +989,65 @@ cudaError_t dispatch_interp_w(const InterpArgs& a, cudaStream_t st) {
   return launch_interp_t<DIM, 0, CG>(a, st);
 }
 
+template <int DIM, int W>
+cudaError_t launch_interp_gm_t(const InterpArgs& a, cudaStream_t st) {
+  if (a.s.M == 0) return cudaSuccess;
+  unsigned blocks = (unsigned)((a.s.M + GBN_THREADS - 1) / GBN_THREADS);
+  if (a.ntr > 1 && a.mode != INTERP_PIPE && a.g.interp_cg != 1)
+    interp_gm_kernel<DIM, W, 4><<<blocks, GBN_THREADS, 0, st>>>(a);
+  else
+    interp_gm_kernel<DIM, W, 1><<<blocks, GBN_THREADS, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int DIM, int S>
+cudaError_t launch_interp_db_t(const InterpArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return cudaSuccess;
+  size_t smem = 2 * (size_t)a.g.tile * sizeof(float2);
+  auto k = interp_db_kernel<DIM, 7, S>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.s.nsub, GBN_THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_interp_wc_t(const InterpArgs& a, cudaStream_t st) {
+  if (a.s.M == 0) return cudaSuccess;
+  const int64_t warps = (a.s.M + 3) / 4;
+  const unsigned blocks = (unsigned)((warps * 32 + GBN_THREADS - 1) / GBN_THREADS);
+  interp_wc_kernel<DIM><<<blocks, GBN_THREADS, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+inline cudaError_t launch_interp_twc(const InterpArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return cudaSuccess;
+  size_t smem = (size_t)a.g.tile * sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(interp_twc3d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  interp_twc3d_kernel<<<a.s.nsub, GBN_THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 template <int DIM>
 cudaError_t dispatch_interp(const InterpArgs& a, cudaStream_t st) {
+  if (a.g.method_interp == 4 && a.g.w == 7) return launch_interp_wc_t<DIM>(a, st);
+  if (DIM == 3 && a.g.method_interp == 5 && a.g.w == 7 && a.s.maxsub <= kTwcMaxSub)
+    return launch_interp_twc(a, st);
+  // default for the w = 7 kernel: double-buffered tiles with register weights
+  if (a.g.method_interp == 3 && a.g.w == 7 && a.s.maxsub <= 2 * GBN_THREADS &&
+      2 * (size_t)a.g.tile * sizeof(float2) <= (size_t)kTileSmemBudget) {
+    if (a.s.maxsub <= GBN_THREADS) return launch_interp_db_t<DIM, 1>(a, st);
+    return launch_interp_db_t<DIM, 2>(a, st);
+  }
+  if (a.g.method_interp == 1) {
+    if (a.g.w == 7) return launch_interp_gm_t<DIM, 7>(a, st);
+    return launch_interp_gm_t<DIM, 0>(a, st);
+  }
   int cg = a.mode == INTERP_PIPE ? 1 : coils_per_pass(a.g, a.ntr);
-  if (cg >= 2) return dispatch_interp_w<DIM, 4>(a, st);
+  if (cg >= 4) return dispatch_interp_w<DIM, 4>(a, st);
+  if (cg == 2) return dispatch_interp_w<DIM, 2>(a, st);
   return dispatch_interp_w<DIM, 1>(a, st);
 }
 
@@ -563,7 +1059,7 @@ inline bool rows_fit(const Geom& g) {
 
 template <int DIM>
 cudaError_t dispatch_spread(const SpreadArgs& a, cudaStream_t st) {
-  if (DIM == 3 && rows_fit(a.g)) {
+  if (DIM == 3 && rows_fit(a.g) && a.g.method_spread != 1) {
     if (a.g.w == 7) return a.ntr > 1 ? launch_spread_rows_t<7, 2>(a, st) : launch_spread_rows_t<7, 1>(a, st);
     return a.ntr > 1 ? launch_spread_rows_t<0, 2>(a, st) : launch_spread_rows_t<0, 1>(a, st);
   }
