@@ -78,6 +78,17 @@ int gbn_plan_info(gbn_plan plan, int* width, double* beta, int64_t* nf, int* bin
 int gbn_plan_device_bytes(gbn_plan plan, int64_t* bytes);
 
 /*
+ * Tune a plan (no counterpart in the reference; used by the autotuner):
+ *   bins          spatial bin extent per axis in fine cells (NULL: keep)
+ *   interp_method 0 shared-memory tiles, 1 direct from the fine grid,
+ *                 3 double-buffered tiles, 4 warp-cooperative direct,
+ *                 5 tiles + warp-cooperative (3D); -1 keeps the current one
+ *   maxsub_cap    largest subproblem (samples per CTA); 0 keeps it
+ * Changing bins or maxsub_cap invalidates the points: call gbn_setpts again.
+ */
+int gbn_plan_tune(gbn_plan plan, const int* bins, int interp_method, int maxsub_cap);
+
+/*
  * Set the non-uniform points: M samples, one float32 device array per image
  * axis (k2 ignored in 2D).  Bin-sorts the points on the device.  Replaces
  * Plan.setpts (finufft.py:55-62, cufinufft.py:94-113).
@@ -149,6 +160,29 @@ int gbn_grad_traj_op(gbn_plan plan, const void* img, const void* smaps, const vo
  */
 int gbn_grad_traj_adj(gbn_plan plan, const void* dx, const void* smaps, const void* y,
                       float* grad, int n_batchs, int n_coils, float scale, gbn_stream stream);
+
+/*
+ * Batches: many independent plans (uneven image size, sample count and coil
+ * count, same dim and kernel width) executed together.  No counterpart in the
+ * reference, whose only batching is n_trans chunks of one trajectory
+ * (base.py:904-914, cufinufft.py:259-269).  Each stage of a batched op / adj
+ * is ONE persistent launch of this library over a work table covering every
+ * instance (pad, interp; zero, spread, crop), plus one cuFFT call per
+ * instance.  Every plan needs gbn_setpts and ntrans >= its coil count.
+ * gbn_batch_bind fixes the device buffers of every instance (image, coil maps
+ * or NULL, k-space, density or NULL, scale, coil count) so that
+ * gbn_batch_op / gbn_batch_adj take only a stream and can be captured in a
+ * CUDA graph:
+ *   op:  ksp_i = scale_i F(smaps_i img_i)      (calibrationless: F(img_i))
+ *   adj: img_i = scale_i sum_c conj(smaps_ic) F^H(d_i ksp_ic)
+ */
+typedef struct gbn_batch_s* gbn_batch;
+int gbn_batch_create(int n, const gbn_plan* plans, gbn_batch* out);
+int gbn_batch_bind(gbn_batch batch, void* const* imgs, const void* const* smaps, void* const* ksps,
+                   const float* const* densities, const float* scales, const int* n_coils);
+int gbn_batch_op(gbn_batch batch, gbn_stream stream);
+int gbn_batch_adj(gbn_batch batch, gbn_stream stream);
+int gbn_batch_destroy(gbn_batch batch);
 
 /*
  * Stage timing.  gbn_profile(plan, 1) clears the counters and records a pair

@@ -41,6 +41,7 @@ SIGNATURES = {
         [_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_i64), ctypes.POINTER(_c_int)],
     ),
     "gbn_plan_device_bytes": (_c_int, [_vp, ctypes.POINTER(_c_i64)]),
+    "gbn_plan_tune": (_c_int, [_vp, ctypes.POINTER(_c_int), _c_int, _c_int]),
     "gbn_setpts": (_c_int, [_vp, _c_i64, _vp, _vp, _vp, _vp]),
     "gbn_op": (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _c_int, _vp]),
     "gbn_adj": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _c_int, _vp]),
@@ -48,6 +49,15 @@ SIGNATURES = {
     "gbn_pipe": (_c_int, [_vp, _vp, _c_int, _c_flt, _vp]),
     "gbn_grad_traj_op": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _vp]),
     "gbn_grad_traj_adj": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _vp]),
+    "gbn_batch_create": (_c_int, [_c_int, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    "gbn_batch_bind": (
+        _c_int,
+        [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+         ctypes.POINTER(_c_flt), ctypes.POINTER(_c_int)],
+    ),
+    "gbn_batch_op": (_c_int, [_vp, _vp]),
+    "gbn_batch_adj": (_c_int, [_vp, _vp]),
+    "gbn_batch_destroy": (_c_int, [_vp]),
     "gbn_profile": (_c_int, [_vp, _c_int]),
     "gbn_profile_read": (_c_int, [_vp, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_i64)]),
     "gbn_norm2_f64": (_c_int, [_vp, _c_i64, _vp, _vp]),

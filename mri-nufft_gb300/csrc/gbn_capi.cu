@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "gbn_batch.cuh"
 #include "gbn_internal.cuh"
 #include "gbn_passes.cuh"
 #include "gbn_sort.cuh"
@@ -194,6 +195,7 @@ struct gbn_plan_s {
   // sort state
   int64_t M = -1, Mcap = 0, subcap = 0;
   int maxsub = 256;
+  int maxsub_cap = 512;
   int nsub = 0;
   SortBuffers sb{};
   int nbins = 0;
@@ -597,7 +599,7 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
     if (M > 0 && (!k0 || !k1 || (p->g.dim == 3 && !k2))) fail(GBN_ERR_ARG, "null coordinates");
     // subproblem size: aim at >= 4 subproblems per SM, 32..1024 samples
     int64_t target = M / (4 * (int64_t)p->nsm);
-    int cap = 512;
+    int cap = p->maxsub_cap;
     if (const char* e = std::getenv("GBN_MAXSUB")) {
       int v = std::atoi(e);
       if (v >= 32 && v <= 65536) cap = v;
@@ -841,6 +843,50 @@ int gbn_profile_read(gbn_plan p, int stage, double* total_ms, int64_t* count) {
   });
 }
 
+int gbn_plan_tune(gbn_plan p, const int* bins, int interp_method, int maxsub_cap) {
+  return guarded(p, [&] {
+    Geom& g = p->g;
+    if (bins) {
+      Geom t = g;
+      for (int d = 0; d < g.dim; ++d) {
+        if (bins[d] < 1 || bins[d] > 64) fail(GBN_ERR_ARG, "bin sizes must be in [1, 64]");
+        t.bs[d] = bins[d] > g.nf[d] ? g.nf[d] : bins[d];
+        t.nb[d] = (g.nf[d] + t.bs[d] - 1) / t.bs[d];
+        t.pd[d] = t.bs[d] + g.w;
+      }
+      t.tile = t.pd[0] * t.pd[1] * t.pd[2];
+      if ((int64_t)t.tile * 8 > kTileSmemBudget) fail(GBN_ERR_ARG, "tile does not fit shared memory");
+      const int nbins = t.nb[0] * t.nb[1] * t.nb[2];
+      if (nbins != p->nbins) {
+        dev_free(p->sb.bin_count);
+        dev_free(p->sb.bin_start);
+        dev_free(p->sb.nsub_bin);
+        dev_free(p->sb.sub_off);
+        dev_free(p->sb.scan_scratch);
+        p->bytes -= (int64_t)p->nbins * 16 + (int64_t)scan_scratch_ints(p->nbins) * 4;
+        p->sb.bin_count = p->sb.bin_start = p->sb.nsub_bin = p->sb.sub_off = p->sb.scan_scratch = nullptr;
+        p->nbins = nbins;
+        p->sb.bin_count = dev_alloc<int>(nbins, p->bytes, "bins");
+        p->sb.bin_start = dev_alloc<int>(nbins, p->bytes, "bins");
+        p->sb.nsub_bin = dev_alloc<int>(nbins, p->bytes, "bins");
+        p->sb.sub_off = dev_alloc<int>(nbins, p->bytes, "bins");
+        p->sb.scan_scratch = dev_alloc<int>(scan_scratch_ints(nbins), p->bytes, "scan");
+      }
+      g = t;
+      p->M = -1;  // points must be set again
+    }
+    if (interp_method >= 0) {
+      if (interp_method > 5 || interp_method == 2) fail(GBN_ERR_ARG, "unknown interpolation method");
+      g.method_interp = interp_method;
+    }
+    if (maxsub_cap > 0) {
+      if (maxsub_cap < 32 || maxsub_cap > 65536) fail(GBN_ERR_ARG, "maxsub_cap must be in [32, 65536]");
+      p->maxsub_cap = maxsub_cap;
+      p->M = -1;
+    }
+  });
+}
+
 int gbn_norm2_f64(const void* x, int64_t n, double* out, gbn_stream stream) {
   g_err.clear();
   if ((!x && n > 0) || !out || n < 0) {
@@ -869,6 +915,181 @@ int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* ou
     g_err = cudaGetErrorString(e);
     return GBN_ERR_CUDA;
   }
+  return GBN_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------------------
+// Batches of independent plans
+// ----------------------------------------------------------------------------
+struct gbn_batch_s {
+  std::vector<gbn_plan> plans;
+  std::vector<BatchInst> h_inst;
+  BatchInst* d_inst = nullptr;
+  WorkItem* d_work = nullptr;
+  BatchTables t{};
+  int device = 0;
+  bool bound = false;
+  ~gbn_batch_s() {
+    dev_free(d_inst);
+    dev_free(d_work);
+  }
+};
+
+extern "C" {
+
+int gbn_batch_create(int n, const gbn_plan* plans, gbn_batch* out) {
+  g_err.clear();
+  if (!out || !plans || n < 1) {
+    g_err = "invalid batch arguments";
+    return GBN_ERR_ARG;
+  }
+  *out = nullptr;
+  gbn_batch b = nullptr;
+  try {
+    DeviceGuard dg(plans[0] ? plans[0]->device : 0);
+    b = new gbn_batch_s();
+    b->device = plans[0] ? plans[0]->device : 0;
+    int64_t tmp = 0;
+    std::vector<WorkItem> sub, fblk, iblk, sblk;
+    size_t tile_bytes = 0;
+    bool w7 = true, rows = true;
+    for (int i = 0; i < n; ++i) {
+      gbn_plan p = plans[i];
+      if (!p) fail(GBN_ERR_ARG, "null plan in batch");
+      if (p->M < 0) fail(GBN_ERR_STATE, "every plan of a batch needs gbn_setpts first");
+      if (p->spread_only) fail(GBN_ERR_ARG, "spread-only plans cannot be batched");
+      if (p->device != b->device) fail(GBN_ERR_ARG, "plans of a batch must share a device");
+      if (p->g.dim != plans[0]->g.dim) fail(GBN_ERR_ARG, "plans of a batch must share dim");
+      w7 = w7 && p->g.w == 7;
+      if (plans[0]->g.w != p->g.w) fail(GBN_ERR_ARG, "plans of a batch must share the kernel width");
+      rows = rows && rows_fit(p->g);
+      b->plans.push_back(p);
+      BatchInst bi{};
+      bi.g = p->g;
+      bi.s = p->sorted();
+      bi.fine = p->fine;
+      for (int d = 0; d < 3; ++d) bi.dec[d] = p->dec[d];
+      b->h_inst.push_back(bi);
+      for (int s = 0; s < p->nsub; ++s) sub.push_back({i, s});
+      for (int64_t k = 0; k < (p->g.G + GBN_THREADS - 1) / GBN_THREADS; ++k) fblk.push_back({i, (int)k});
+      for (int64_t k = 0; k < (p->g.Nimg + GBN_THREADS - 1) / GBN_THREADS; ++k) iblk.push_back({i, (int)k});
+      for (int64_t k = 0; k < (p->M + GBN_THREADS - 1) / GBN_THREADS; ++k) sblk.push_back({i, (int)k});
+      size_t tb = (size_t)p->g.tile * sizeof(float2);
+      if (tb > tile_bytes) tile_bytes = tb;
+    }
+    std::vector<WorkItem> all;
+    all.insert(all.end(), sub.begin(), sub.end());
+    all.insert(all.end(), fblk.begin(), fblk.end());
+    all.insert(all.end(), iblk.begin(), iblk.end());
+    all.insert(all.end(), sblk.begin(), sblk.end());
+    b->d_inst = dev_alloc<BatchInst>(n, tmp, "batch instances");
+    b->d_work = dev_alloc<WorkItem>(all.size(), tmp, "batch work tables");
+    if (!all.empty())
+      ck(cudaMemcpy(b->d_work, all.data(), all.size() * sizeof(WorkItem), cudaMemcpyHostToDevice),
+         "copy work tables");
+    BatchTables& t = b->t;
+    t.inst = b->d_inst;
+    t.sub = b->d_work;
+    t.nsub = (int)sub.size();
+    t.fblk = b->d_work + sub.size();
+    t.nfblk = (int)fblk.size();
+    t.iblk = t.fblk + fblk.size();
+    t.niblk = (int)iblk.size();
+    t.sblk = t.iblk + iblk.size();
+    t.nsblk = (int)sblk.size();
+    t.dim = plans[0]->g.dim;
+    t.w7 = w7 ? 1 : 0;
+    t.rows = rows ? 1 : 0;
+    t.tile_bytes = tile_bytes;
+    t.grid = plans[0]->nsm * 4;
+    ck(batch_prepare(t), "batch kernel attributes");
+    *out = b;
+    return GBN_OK;
+  } catch (const Fail& e) {
+    delete b;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    delete b;
+    g_err = "host allocation failed";
+    return GBN_ERR_NOMEM;
+  }
+}
+
+int gbn_batch_bind(gbn_batch b, void* const* imgs, const void* const* smaps, void* const* ksps,
+                   const float* const* densities, const float* scales, const int* n_coils) {
+  g_err.clear();
+  if (!b || !imgs || !ksps || !scales || !n_coils) {
+    g_err = "invalid batch bind arguments";
+    return GBN_ERR_ARG;
+  }
+  try {
+    DeviceGuard dg(b->device);
+    for (size_t i = 0; i < b->plans.size(); ++i) {
+      gbn_plan p = b->plans[i];
+      BatchInst& bi = b->h_inst[i];
+      if (n_coils[i] < 1 || n_coils[i] > p->ntrans)
+        fail(GBN_ERR_ARG, "instance " + std::to_string(i) + ": n_coils must be in [1, plan ntrans]");
+      if (!imgs[i] || (!ksps[i] && p->M > 0)) fail(GBN_ERR_ARG, "null buffer in batch bind");
+      bi.img = static_cast<float2*>(imgs[i]);
+      bi.smaps = smaps ? static_cast<const float2*>(smaps[i]) : nullptr;
+      bi.ksp = static_cast<float2*>(ksps[i]);
+      bi.density = densities ? densities[i] : nullptr;
+      bi.scale = scales[i];
+      bi.ncoils = n_coils[i];
+    }
+    ck(cudaMemcpy(b->d_inst, b->h_inst.data(), b->h_inst.size() * sizeof(BatchInst),
+                  cudaMemcpyHostToDevice),
+       "copy batch descriptors");
+    b->bound = true;
+    return GBN_OK;
+  } catch (const Fail& e) {
+    return e.code;
+  }
+}
+
+static int batch_run(gbn_batch b, bool adjoint, gbn_stream stream) {
+  g_err.clear();
+  if (!b) {
+    g_err = "null batch";
+    return GBN_ERR_ARG;
+  }
+  if (!b->bound) {
+    g_err = "gbn_batch_bind has not been called";
+    return GBN_ERR_STATE;
+  }
+  try {
+    DeviceGuard dg(b->device);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (!adjoint) {
+      ck(batch_pad(b->t, st), "batch pad");
+      for (size_t i = 0; i < b->plans.size(); ++i)
+        b->plans[i]->exec_fft(b->h_inst[i].ncoils, b->plans[i]->fine, -1, st);
+      ck(batch_interp(b->t, st), "batch interp");
+    } else {
+      ck(batch_zero(b->t, st), "batch zero");
+      ck(batch_spread(b->t, st), "batch spread");
+      for (size_t i = 0; i < b->plans.size(); ++i)
+        b->plans[i]->exec_fft(b->h_inst[i].ncoils, b->plans[i]->fine, +1, st);
+      ck(batch_crop(b->t, st), "batch crop");
+    }
+    return GBN_OK;
+  } catch (const Fail& e) {
+    return e.code;
+  }
+}
+
+int gbn_batch_op(gbn_batch b, gbn_stream stream) { return batch_run(b, false, stream); }
+int gbn_batch_adj(gbn_batch b, gbn_stream stream) { return batch_run(b, true, stream); }
+
+int gbn_batch_destroy(gbn_batch b) {
+  if (!b) return GBN_OK;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != b->device) cudaSetDevice(b->device);
+  delete b;
+  if (prev >= 0 && prev != b->device) cudaSetDevice(prev);
   return GBN_OK;
 }
 

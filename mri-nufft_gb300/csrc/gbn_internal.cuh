@@ -161,4 +161,10 @@ inline int coils_per_pass(const Geom& g, int ntr) {
   return cg;
 }
 
+// 3D tiles up to 16 x 16 x 16 cells use the row spreading kernel (two coils
+// per pass); 2D, and wider kernels, use the sample-driven global-atomic one.
+inline bool rows_fit(const Geom& g) {
+  return g.dim == 3 && g.w <= 8 && g.pd[0] <= 16 && g.pd[1] <= 16 && g.pd[2] <= 16;
+}
+
 }  // namespace gbn

@@ -129,12 +129,10 @@ __device__ __forceinline__ void load_tiles(float2* tile, const float2* __restric
 // Interpolation
 // ---------------------------------------------------------------------------
 template <int DIM, int W, int CG>
-__global__ void __launch_bounds__(GBN_THREADS)
-interp_kernel(InterpArgs a) {
+__device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) {
   constexpr int WM = WidthTraits<W>::WM;
   extern __shared__ float2 tile[];
   const Geom& g = a.g;
-  const int sub = blockIdx.x;
   const int b = a.s.sub_bin[sub];
   const int p0 = a.s.sub_start[sub];
   const int cnt = a.s.sub_count[sub];
@@ -236,6 +234,12 @@ GBN_UNROLL
     }
     __syncthreads();
   }
+}
+
+template <int DIM, int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS)
+interp_kernel(InterpArgs a) {
+  interp_body<DIM, W, CG>(a, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -695,15 +699,13 @@ interp_twc3d_kernel(InterpArgs a) {
 constexpr int kRowBatch = 256;
 
 template <int W, int CG>
-__global__ void __launch_bounds__(GBN_THREADS, 2)
-spread_rows3d_kernel(SpreadArgs a) {
+__device__ __forceinline__ void spread_rows3d_body(const SpreadArgs& a, const int sub) {
   constexpr int WM = W > 0 ? W : 8;
   __shared__ int s_a0[kRowBatch], s_a1[kRowBatch];
   __shared__ float s_w0[kRowBatch][8], s_w1[kRowBatch][8];
   __shared__ __align__(16) float s_w2[kRowBatch][16];
   __shared__ float2 s_c[CG][kRowBatch];
   const Geom& g = a.g;
-  const int sub = blockIdx.x;
   const int b = a.s.sub_bin[sub];
   const int p0 = a.s.sub_start[sub];
   const int cnt = a.s.sub_count[sub];
@@ -807,6 +809,12 @@ spread_rows3d_kernel(SpreadArgs a) {
   }
 }
 
+template <int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS, 2)
+spread_rows3d_kernel(SpreadArgs a) {
+  spread_rows3d_body<W, CG>(a, blockIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Spreading, sample-driven kernel with global vector atomics (2D, and any
 // width the row kernel does not cover).  Threads take consecutive sorted
@@ -814,11 +822,9 @@ spread_rows3d_kernel(SpreadArgs a) {
 // same L2 sectors.
 // ---------------------------------------------------------------------------
 template <int DIM, int W>
-__global__ void __launch_bounds__(GBN_THREADS)
-spread_gm_kernel(SpreadArgs a) {
+__device__ __forceinline__ void spread_gm_body(const SpreadArgs& a, const int64_t pos) {
   constexpr int WM = WidthTraits<W>::WM;
   const Geom& g = a.g;
-  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (pos >= a.s.M) return;
   const int w = W > 0 ? W : g.w;
   const int WL = W > 0 ? W : w;
@@ -859,6 +865,12 @@ GBN_UNROLL
       }
     }
   }
+}
+
+template <int DIM, int W>
+__global__ void __launch_bounds__(GBN_THREADS)
+spread_gm_kernel(SpreadArgs a) {
+  spread_gm_body<DIM, W>(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1051,11 +1063,6 @@ cudaError_t dispatch_interp(const InterpArgs& a, cudaStream_t st) {
   return dispatch_interp_w<DIM, 1>(a, st);
 }
 
-// 3D tiles up to 16 x 16 x 16 cells use the row kernel (two coils per pass);
-// 2D, and wider kernels, use the sample-driven global-atomic kernel.
-inline bool rows_fit(const Geom& g) {
-  return g.dim == 3 && g.w <= 8 && g.pd[0] <= 16 && g.pd[1] <= 16 && g.pd[2] <= 16;
-}
 
 template <int DIM>
 cudaError_t dispatch_spread(const SpreadArgs& a, cudaStream_t st) {

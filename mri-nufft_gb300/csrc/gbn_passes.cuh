@@ -27,6 +27,107 @@ struct CropArgs {
   float scale;
 };
 
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // conj(a) * b
+  return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// pad pass for fine cell idx (see gbn_passes.cu)
+template <int DIM>
+__device__ __forceinline__ void pad_body(const PadArgs& a, const int64_t idx) {
+  const Geom& g = a.g;
+  if (idx >= g.G) return;
+  int m[3] = {0, 0, 0};
+  {
+    int64_t r = idx;
+    for (int d = DIM - 1; d >= 0; --d) {
+      m[d] = (int)(r % g.nf[d]);
+      r /= g.nf[d];
+    }
+  }
+  bool inside = true;
+  int64_t ii = 0;
+  float f = a.scale;
+  for (int d = 0; d < DIM; ++d) {
+    int h = g.n[d] / 2;              // floor(N/2)
+    int hi = g.n[d] - h;             // modes 0 .. hi-1 at the start
+    int n;
+    if (m[d] < hi) n = m[d];
+    else if (m[d] >= g.nf[d] - h) n = m[d] - g.nf[d];
+    else { inside = false; break; }
+    int i = n + h;
+    ii = ii * g.n[d] + i;
+    f *= a.dec[d][i];
+  }
+  if (!inside) {
+    for (int c = 0; c < a.ntr; ++c) a.fine[(int64_t)c * g.G + idx] = make_float2(0.f, 0.f);
+    return;
+  }
+  if (a.smaps) {
+    float2 x = a.img[ii];
+    if (a.conj_in) x = conjf2(x);
+    for (int c = 0; c < a.ntr; ++c) {
+      float2 s = a.smaps[(int64_t)c * g.Nimg + ii];
+      if (a.conj_in) s = conjf2(s);
+      float2 v = cmul(x, s);
+      a.fine[(int64_t)c * g.G + idx] = make_float2(v.x * f, v.y * f);
+    }
+  } else {
+    for (int c = 0; c < a.ntr; ++c) {
+      float2 x = a.img[(int64_t)c * g.Nimg + ii];
+      if (a.conj_in) x = conjf2(x);
+      a.fine[(int64_t)c * g.G + idx] = make_float2(x.x * f, x.y * f);
+    }
+  }
+}
+
+// crop pass for image pixel idx (see gbn_passes.cu)
+template <int DIM>
+__device__ __forceinline__ void crop_body(const CropArgs& a, const int64_t idx) {
+  const Geom& g = a.g;
+  if (idx >= g.Nimg) return;
+  int64_t r = idx;
+  int64_t mlin = 0;
+  float f = a.scale;
+  int i[3] = {0, 0, 0};
+  for (int d = DIM - 1; d >= 0; --d) {
+    i[d] = (int)(r % g.n[d]);
+    r /= g.n[d];
+  }
+  for (int d = 0; d < DIM; ++d) {
+    int n = i[d] - g.n[d] / 2;
+    int m = n < 0 ? n + g.nf[d] : n;
+    mlin = mlin * g.nf[d] + m;
+    f *= a.dec[d][i[d]];
+  }
+  if (a.smaps) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < a.ntr; ++c) {
+      float2 v = a.fine[(int64_t)c * g.G + mlin];
+      float2 s = a.smaps[(int64_t)c * g.Nimg + idx];
+      float2 p = cmulc(s, v);
+      acc.x += p.x;
+      acc.y += p.y;
+    }
+    acc.x *= f;
+    acc.y *= f;
+    if (a.accumulate) {
+      float2 o = a.out[idx];
+      acc.x += o.x;
+      acc.y += o.y;
+    }
+    a.out[idx] = acc;
+  } else {
+    for (int c = 0; c < a.ntr; ++c) {
+      float2 v = a.fine[(int64_t)c * g.G + mlin];
+      a.out[(int64_t)c * g.Nimg + idx] = make_float2(v.x * f, v.y * f);
+    }
+  }
+}
+
 cudaError_t launch_pad(const PadArgs& a, cudaStream_t st);
 cudaError_t launch_crop(const CropArgs& a, cudaStream_t st);
 cudaError_t launch_norm2(const float2* x, int64_t n, double* out, cudaStream_t st);

@@ -81,6 +81,26 @@ class NufftPlan:
         _lib.check(self.lib.gbn_plan_device_bytes(self._h, ctypes.byref(b)), "gbn_plan_device_bytes")
         return b.value
 
+    # ---------------------------------------------------------------- tuning
+    METHODS = {"tile": 0, "direct": 1, "double_buffered": 3, "warp_direct": 4, "warp_tile": 5}
+
+    def tune(self, bins=None, interp=None, maxsub_cap=0):
+        """Set bin sizes (fine cells per axis), interpolation method and the
+        largest subproblem; points must be set again afterwards."""
+        b = None if bins is None else (ctypes.c_int * self.ndim)(*[int(v) for v in bins])
+        m = -1 if interp is None else self.METHODS[interp]
+        _lib.check(self.lib.gbn_plan_tune(self._h, b, m, int(maxsub_cap)), "gbn_plan_tune")
+        if self._coords is not None and (bins is not None or maxsub_cap):
+            self._reset_points()
+
+    def _reset_points(self):
+        cols = self._coords
+        M = self.n_samples
+        _lib.check(
+            self.lib.gbn_setpts(self._h, M, _ptr(cols[0]), _ptr(cols[1]), _ptr(cols[2]), self.stream),
+            "gbn_setpts",
+        )
+
     # ------------------------------------------------------------- profiling
     def profile(self, enable: bool = True):
         """Start (clear) or stop per-stage CUDA-event timing."""

@@ -129,3 +129,27 @@ def config2(n_spokes: int = 4096, n_samples: int = 512, n_coils: int = 16, N: in
     shape = (N, N, N)
     traj = kooshball_3d(n_spokes, n_samples).reshape(-1, 3).astype(np.float32)
     return traj, shape, phantom(shape, seed=0), coil_maps(shape, n_coils, seed=0)
+
+
+def config3(n_instances: int = 32, seed: int = 0):
+    """Uneven 2D instances: grids from {128, 192, 256, 320, 384}^2, even
+    instances variable-density (Galilean) spirals with Nc in [16, 64] and Ns in
+    [1024, 4096], odd instances radial with Nc in [64, 256] and Ns in
+    [256, 1024], coil counts from {1, 4, 8, 16, 32}; seeded phantoms and maps."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_instances):
+        N = int(rng.choice([128, 192, 256, 320, 384]))
+        C = int(rng.choice([1, 4, 8, 16, 32]))
+        if i % 2 == 0:
+            traj = spiral_2d(int(rng.integers(16, 65)), int(rng.integers(1024, 4097)), power=2)
+        else:
+            traj = radial_2d(int(rng.integers(64, 257)), int(rng.integers(256, 1025)))
+        shape = (N, N)
+        out.append({
+            "samples": traj.reshape(-1, 2).astype(np.float32),
+            "shape": shape,
+            "smaps": coil_maps(shape, C, seed=seed + i),
+            "image": phantom(shape, seed=seed + i),
+        })
+    return out
