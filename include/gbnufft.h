@@ -217,6 +217,32 @@ int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* ou
                  gbn_stream stream);
 
 /*
+ * Device-side solver steps, so that a whole CG reconstruction runs without a
+ * host synchronisation (the served form keeps many solves in flight).
+ *
+ * gbn_cg_update: one Polak-Ribiere step of extras/optim.py:866-881 on complex64
+ *   vectors of length n.  state (doubles, device) holds [0,1] dot(g_new, g_new),
+ *   [2,3] dot(g_new, g), [4,5] dot(g, g) (numpy's non-conjugating dot, as from
+ *   gbn_dotu_f64), [6] |g_new|^2 (gbn_norm2_f64), [7] done flag.  Unless done
+ *   or |g_new| <= tol (then done is set, the reference's early exit):
+ *   beta = max(0, (dot(g_new,g_new) - dot(g_new,g)) / dot(g,g)) under numpy's
+ *   complex ordering,
+ *   velocity = g_new + beta velocity, image -= velocity / L, grad = g_new.
+ *   lipschitz is a device float.
+ * gbn_power_step: the normalisation of one power-method iteration
+ *   (operators/base.py:1202-1209): state [0] |x_new|^2, [1] previous norm,
+ *   [2] current estimate, [3] converged flag; x = x_new / |x_new| and the
+ *   estimate goes to *lipschitz, until |previous - current| < 1e-6.
+ * gbn_scale_ratio: x *= sqrt(num2 / den2) with both squared norms on the
+ *   device (the scaling of _scaled_dcp, extras/optim.py:151-165).
+ */
+int gbn_cg_update(int64_t n, const void* grad_new, void* grad, void* velocity, void* image,
+                  double* state, const float* lipschitz, float tol, gbn_stream stream);
+int gbn_power_step(int64_t n, const void* x_new, void* x, double* state, float* lipschitz,
+                   gbn_stream stream);
+int gbn_scale_ratio(int64_t n, void* x, const double* num2, const double* den2, gbn_stream stream);
+
+/*
  * Pipe density iterations that allocate nothing.  No counterpart in the
  * reference: it is the gbn_pipe iteration for callers that cannot allocate
  * device memory at the time they need it (a process whose device memory is

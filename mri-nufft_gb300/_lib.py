@@ -62,6 +62,9 @@ SIGNATURES = {
     "gbn_profile_read": (_c_int, [_vp, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_i64)]),
     "gbn_norm2_f64": (_c_int, [_vp, _c_i64, _vp, _vp]),
     "gbn_dotu_f64": (_c_int, [_vp, _vp, _c_i64, _c_int, _vp, _vp]),
+    "gbn_cg_update": (_c_int, [_c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_flt, _vp]),
+    "gbn_power_step": (_c_int, [_c_i64, _vp, _vp, _vp, _vp, _vp]),
+    "gbn_scale_ratio": (_c_int, [_c_i64, _vp, _vp, _vp, _vp]),
     "gbn_pipe_static": (
         _c_int,
         [_c_int, ctypes.POINTER(_c_i64), _c_dbl, _c_dbl, _c_i64, _vp, _vp, _vp, _vp, _c_int, _c_flt, _vp],

@@ -887,6 +887,47 @@ int gbn_plan_tune(gbn_plan p, const int* bins, int interp_method, int maxsub_cap
   });
 }
 
+static int simple_status(cudaError_t e) {
+  if (e == cudaSuccess) return GBN_OK;
+  g_err = cudaGetErrorString(e);
+  return GBN_ERR_CUDA;
+}
+
+int gbn_cg_update(int64_t n, const void* grad_new, void* grad, void* velocity, void* image,
+                  double* state, const float* lipschitz, float tol, gbn_stream stream) {
+  g_err.clear();
+  if (n < 0 || !state || !lipschitz || (n > 0 && (!grad_new || !grad || !velocity || !image))) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  return simple_status(launch_cg_update(n, static_cast<const float2*>(grad_new),
+                                        static_cast<float2*>(grad), static_cast<float2*>(velocity),
+                                        static_cast<float2*>(image), state, lipschitz, tol,
+                                        reinterpret_cast<cudaStream_t>(stream)));
+}
+
+int gbn_power_step(int64_t n, const void* x_new, void* x, double* state, float* lipschitz,
+                   gbn_stream stream) {
+  g_err.clear();
+  if (n < 0 || !state || !lipschitz || (n > 0 && (!x_new || !x))) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  return simple_status(launch_power_step(n, static_cast<const float2*>(x_new),
+                                         static_cast<float2*>(x), state, lipschitz,
+                                         reinterpret_cast<cudaStream_t>(stream)));
+}
+
+int gbn_scale_ratio(int64_t n, void* x, const double* num2, const double* den2, gbn_stream stream) {
+  g_err.clear();
+  if (n < 0 || !num2 || !den2 || (n > 0 && !x)) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  return simple_status(launch_scale_ratio(n, static_cast<float2*>(x), num2, den2,
+                                          reinterpret_cast<cudaStream_t>(stream)));
+}
+
 int gbn_norm2_f64(const void* x, int64_t n, double* out, gbn_stream stream) {
   g_err.clear();
   if ((!x && n > 0) || !out || n < 0) {

@@ -118,3 +118,103 @@ cudaError_t launch_dotu(const float2* a, const float2* b, int64_t n, int conj_a,
 }
 
 }  // namespace gbn
+
+// ---------------------------------------------------------------------------
+// Device-side solver updates (no host synchronisation inside a solve)
+// ---------------------------------------------------------------------------
+namespace gbn {
+
+// state layout (doubles): [0,1] dot(g_new, g_new)  [2,3] dot(g_new, g)
+//                         [4,5] dot(g, g)          [6] |g_new|^2  [7] done flag
+__global__ void cg_update_kernel(int64_t n, const float2* __restrict__ gnew, float2* grad,
+                                 float2* vel, float2* img, const double* st, const float* L,
+                                 float tol) {
+  if (st[7] != 0.0) return;
+  const double nrm = sqrt(st[6]);
+  if (!(nrm > (double)tol)) return;  // the state kernel marks the solve done
+  // beta = (dot(gn, gn) - dot(gn, g)) / dot(g, g) (complex), then numpy's
+  // max(0, beta): kept when Re > 0 or (Re == 0 and Im > 0), else 0
+  const double nr = st[0] - st[2], ni = st[1] - st[3], dr = st[4], di = st[5];
+  const double dd = dr * dr + di * di;
+  double br = (nr * dr + ni * di) / dd;
+  double bi = (ni * dr - nr * di) / dd;
+  if (!(br > 0.0 || (br == 0.0 && bi > 0.0))) {
+    br = 0.0;
+    bi = 0.0;
+  }
+  const float fbr = (float)br, fbi = (float)bi, invL = 1.0f / *L;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 g = gnew[i];
+    const float2 v = vel[i];
+    const float2 nv = make_float2(g.x + fbr * v.x - fbi * v.y, g.y + fbr * v.y + fbi * v.x);
+    vel[i] = nv;
+    float2 x = img[i];
+    x.x -= nv.x * invL;
+    x.y -= nv.y * invL;
+    img[i] = x;
+    grad[i] = g;
+  }
+}
+
+__global__ void cg_state_kernel(double* st, float tol) {
+  if (st[7] == 0.0 && !(sqrt(st[6]) > (double)tol)) st[7] = 1.0;
+}
+
+// power method state (doubles): [0] |x_new|^2 [1] x_norm [2] L [3] converged
+__global__ void power_normalize_kernel(int64_t n, const float2* __restrict__ xnew, float2* x,
+                                       const double* st) {
+  if (st[3] != 0.0) return;
+  const float inv = (float)(1.0 / sqrt(st[0]));
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = xnew[i];
+    x[i] = make_float2(v.x * inv, v.y * inv);
+  }
+}
+
+__global__ void power_state_kernel(double* st, float* L) {
+  if (st[3] != 0.0) return;
+  const double nn = sqrt(st[0]);
+  st[2] = nn;
+  *L = (float)nn;
+  if (fabs(st[1] - nn) < 1e-6) st[3] = 1.0;
+  st[1] = nn;
+}
+
+// x *= sqrt(num2 / den2), both squared norms on the device
+__global__ void scale_ratio_kernel(int64_t n, float2* x, const double* num2, const double* den2) {
+  const float s = (float)sqrt(*num2 / *den2);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float2 v = x[i];
+    x[i] = make_float2(v.x * s, v.y * s);
+  }
+}
+
+static unsigned elem_blocks(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (unsigned)(b < 1216 ? (b < 1 ? 1 : b) : 1216);
+}
+
+cudaError_t launch_cg_update(int64_t n, const float2* gnew, float2* grad, float2* vel, float2* img,
+                             double* st, const float* L, float tol, cudaStream_t s) {
+  cg_update_kernel<<<elem_blocks(n), 256, 0, s>>>(n, gnew, grad, vel, img, st, L, tol);
+  cg_state_kernel<<<1, 1, 0, s>>>(st, tol);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_power_step(int64_t n, const float2* xnew, float2* x, double* st, float* L,
+                              cudaStream_t s) {
+  power_normalize_kernel<<<elem_blocks(n), 256, 0, s>>>(n, xnew, x, st);
+  power_state_kernel<<<1, 1, 0, s>>>(st, L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale_ratio(int64_t n, float2* x, const double* num2, const double* den2,
+                               cudaStream_t s) {
+  scale_ratio_kernel<<<elem_blocks(n), 256, 0, s>>>(n, x, num2, den2);
+  return cudaGetLastError();
+}
+
+}  // namespace gbn

@@ -133,5 +133,11 @@ cudaError_t launch_crop(const CropArgs& a, cudaStream_t st);
 cudaError_t launch_norm2(const float2* x, int64_t n, double* out, cudaStream_t st);
 cudaError_t launch_dotu(const float2* a, const float2* b, int64_t n, int conj_a, double* out,
                         cudaStream_t st);
+cudaError_t launch_cg_update(int64_t n, const float2* gnew, float2* grad, float2* vel, float2* img,
+                             double* st, const float* L, float tol, cudaStream_t s);
+cudaError_t launch_power_step(int64_t n, const float2* xnew, float2* x, double* st, float* L,
+                              cudaStream_t s);
+cudaError_t launch_scale_ratio(int64_t n, float2* x, const double* num2, const double* den2,
+                               cudaStream_t s);
 
 }  // namespace gbn

@@ -1,0 +1,312 @@
+"""Served form: continuous batching of CG reconstructions on one GPU.
+
+``ReconServer`` accepts CG data-consistency reconstructions (the work of
+``pinv_solver(optim="cg")``, ``extras/optim.py:801-902``, with its power-method
+Lipschitz estimate, ``operators/base.py:1155-1221``) of different dims, sizes
+and coil counts as they arrive:
+
+* admission: a request is admitted when a slot is free and its device bytes
+  fit the HBM budget next to the requests already on the GPU; otherwise it
+  waits in the queue;
+* residency: sorted trajectories stay on the device in a pool of plans keyed
+  by trajectory (requests of one protocol reuse the bin sort), and each
+  admitted request keeps its coil maps, k-space and CG state on the device;
+* continuous batching: every scheduling tick issues the next unit of work
+  (one power iteration or one CG iteration) of every admitted request, each
+  request on its own CUDA stream, so the work of many requests overlaps on
+  the device; a request that finishes frees its slot and memory at once and
+  a waiting one is admitted at the next tick;
+* no host synchronisation inside a solve: the power-method normalisation,
+  the CG step (Polak-Ribiere beta with numpy's complex ``max(0, beta)``, the
+  ``tol`` early exit) and their FP64 reductions run on the device
+  (``gbn_power_step``, ``gbn_cg_update``, ``gbn_dotu_f64``, ``gbn_norm2_f64``).
+
+Each result equals the same request run alone (and ``MRIGB300.pinv_solver``
+with the same power-method start vector) up to float rounding.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import time
+from collections import defaultdict, deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _array, _lib
+from ._traj import proper_trajectory
+from .params import fine_cells
+from .plan import NufftPlan, _ptr
+
+
+@dataclass
+class ReconRequest:
+    """One CG reconstruction (SENSE when ``smaps`` is given)."""
+
+    rid: int
+    samples: object           # (M, d), unit or radians
+    shape: tuple
+    kspace: object            # (C, M)
+    smaps: object = None      # (C, *shape)
+    density: object = None    # (M,)
+    max_iter: int = 10
+    tol: float = 1e-4
+    seed: int = 0             # power-method start vector
+    traj_key: object = None   # requests with equal keys share a sorted trajectory
+    arrival: float = 0.0
+    result: torch.Tensor = None
+    t_admit: float = None
+    t_done: float = None
+    lipschitz: float = None
+
+    @property
+    def n_coils(self):
+        return int(self.kspace.shape[0]) if self.kspace.ndim > 1 else 1
+
+
+def start_vector(shape, seed):
+    """1j * U[0,1) + U[0,1), the start vector of the GPU backends'
+    ``get_lipschitz_cst`` (cufinufft.py:1265-1266), from a seeded generator."""
+    rs = np.random.RandomState(seed)
+    x = 1j * rs.random_sample(shape).astype(np.complex64)
+    x += rs.random_sample(shape).astype(np.complex64)
+    return x
+
+
+def request_bytes(shape, M, C, eps=1e-6):
+    """Device bytes of one admitted request: plan (fine grids, sort tables),
+    coil maps, k-space, CG / power-method vectors."""
+    G = fine_cells(shape, eps)
+    N = int(np.prod(shape))
+    d = len(shape)
+    plan = 8 * C * G + M * (12 + 4 * d) + 8 * C * M
+    data = 8 * C * N + 8 * C * M + 4 * M
+    state = 8 * N * 7
+    return int(plan + data + state)
+
+
+class _Solve:
+    """Device state and unit generator of one admitted request."""
+
+    def __init__(self, server, req, plan, stream):
+        self.server, self.req, self.plan, self.stream = server, req, plan, stream
+        self.dev = server.device
+        self.lib = server.lib
+        shape = tuple(int(v) for v in req.shape)
+        self.shape = shape
+        C = req.n_coils
+        self.C = C
+        with torch.cuda.stream(stream):
+            self.y = _array.to_tensor(req.kspace, self.dev, torch.complex64).reshape(C, -1)
+            self.smaps = (None if req.smaps is None
+                          else _array.to_tensor(req.smaps, self.dev, torch.complex64).reshape(C, *shape))
+            self.dens = (None if req.density is None
+                         else _array.to_tensor(req.density, self.dev, torch.float32).reshape(-1))
+            self.x0 = torch.from_numpy(start_vector(shape, req.seed)).to(self.dev, non_blocking=True)
+        self.M = self.y.shape[1]
+        self.scale = 1.0 / float(np.sqrt(np.prod(shape) * 2 ** len(shape)))
+        self.bytes = request_bytes(shape, self.M, C, server.eps)
+        self.gen = self._units()
+        self.event = None
+
+    def _st(self):
+        return ctypes.c_void_p(self.stream.cuda_stream)
+
+    def _ck(self, status, what):
+        _lib.check(status, what)
+
+    def _units(self):
+        dev, plan, shape, C = self.dev, self.plan, self.shape, self.C
+        n = int(np.prod(shape))
+        sense = self.smaps is not None
+        img_shape = (1, *shape) if sense else (C, *shape)
+        nimg = int(np.prod(img_shape))
+        f32 = dict(dtype=torch.float32, device=dev)
+        c64 = dict(dtype=torch.complex64, device=dev)
+        f64 = dict(dtype=torch.float64, device=dev)
+        L = torch.zeros(1, **f32)
+        pst = torch.zeros(4, **f64)
+        x = torch.empty((1, *shape), **c64)
+        xn = torch.empty((1, *shape), **c64)
+        ktmp = torch.empty((1, self.M), **c64)
+        # -- power method on the single-coil, map-free operator with density
+        self._ck(self.lib.gbn_norm2_f64(_ptr(self.x0), n, _ptr(pst), self._st()), "norm2")
+        self._ck(self.lib.gbn_power_step(n, _ptr(self.x0), _ptr(x), _ptr(pst), _ptr(L), self._st()),
+                 "power step")
+        yield
+        for _ in range(10):
+            plan.op(x, None, ktmp, 1, 1, self.scale)
+            plan.adj(ktmp, self.dens, None, xn, 1, 1, self.scale)
+            self._ck(self.lib.gbn_norm2_f64(_ptr(xn), n, _ptr(pst), self._st()), "norm2")
+            self._ck(self.lib.gbn_power_step(n, _ptr(xn), _ptr(x), _ptr(pst), _ptr(L), self._st()),
+                     "power step")
+            yield
+        self.L = L
+        # -- start image: scaled density-compensated adjoint (optim.py:151-165)
+        image = torch.zeros(img_shape, **c64)
+        y = self.y.reshape(1, C, self.M)
+        if self.dens is not None:
+            plan.adj(y, self.dens, self.smaps, image, 1, C, self.scale)
+            yy = torch.empty((1, C, self.M), **c64)
+            plan.op(image.reshape(1 if sense else C, *shape), self.smaps, yy, 1, C, self.scale)
+            nrm = torch.empty(2, **f64)
+            self._ck(self.lib.gbn_norm2_f64(_ptr(y), y.numel(), _ptr(nrm[0:1]), self._st()), "norm2")
+            self._ck(self.lib.gbn_norm2_f64(_ptr(yy), yy.numel(), _ptr(nrm[1:2]), self._st()), "norm2")
+            self._ck(self.lib.gbn_scale_ratio(nimg, _ptr(image), _ptr(nrm[0:1]), _ptr(nrm[1:2]),
+                                              self._st()), "scale")
+            yield
+        # -- CG iterations without density (optim.py:838-842)
+        grad = torch.empty(img_shape, **c64)
+        gnew = torch.empty(img_shape, **c64)
+        xin = image.reshape(1 if sense else C, *shape)
+        plan.dc(xin, y, None, self.smaps, grad, 1, C, self.scale)
+        velocity = grad / L
+        image -= velocity
+        st = torch.zeros(8, **f64)
+        yield
+        for _ in range(self.req.max_iter):
+            plan.dc(xin, y, None, self.smaps, gnew, 1, C, self.scale)
+            s = self._st()
+            self._ck(self.lib.gbn_dotu_f64(_ptr(gnew), _ptr(gnew), nimg, 0, _ptr(st[0:2]), s), "dot")
+            self._ck(self.lib.gbn_dotu_f64(_ptr(gnew), _ptr(grad), nimg, 0, _ptr(st[2:4]), s), "dot")
+            self._ck(self.lib.gbn_dotu_f64(_ptr(grad), _ptr(grad), nimg, 0, _ptr(st[4:6]), s), "dot")
+            self._ck(self.lib.gbn_norm2_f64(_ptr(gnew), nimg, _ptr(st[6:7]), s), "norm2")
+            self._ck(self.lib.gbn_cg_update(nimg, _ptr(gnew), _ptr(grad), _ptr(velocity), _ptr(image),
+                                            _ptr(st), _ptr(L), float(self.req.tol), s), "cg update")
+            yield
+        self.image = image
+        self.event = torch.cuda.Event()
+        self.event.record(self.stream)
+
+    def step(self):
+        """Issue the next unit; False once every unit is issued."""
+        with torch.cuda.stream(self.stream):
+            try:
+                next(self.gen)
+                return True
+            except StopIteration:
+                return False
+
+
+class ReconServer:
+    """Continuous-batching CG reconstruction service on one GPU."""
+
+    def __init__(self, hbm_budget_bytes=150e9, max_active=32, device=None, eps=1e-6):
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.budget = float(hbm_budget_bytes)
+        self.max_active = int(max_active)
+        self.eps = eps
+        self.lib = _lib.load()
+        self.queue = deque()
+        self.active = []
+        self.finishing = []
+        self.done = []
+        self.used = 0
+        self.plans = defaultdict(list)   # (traj key, shape, coils) -> free sorted plans
+        self.plan_bytes = 0
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(self.max_active)]
+        self.free_streams = list(range(self.max_active))
+        self.t0 = time.perf_counter()
+
+    def now(self):
+        return time.perf_counter() - self.t0
+
+    def submit(self, req: ReconRequest):
+        self.queue.append(req)
+
+    def _acquire_plan(self, req, stream):
+        shape = tuple(int(v) for v in req.shape)
+        key = (req.traj_key if req.traj_key is not None else ("rid", req.rid), shape, req.n_coils)
+        pool = self.plans[key]
+        if pool:
+            return key, pool.pop()
+        with torch.cuda.stream(stream):
+            plan = NufftPlan(shape, eps=self.eps, ntrans=req.n_coils, device=self.device.index)
+            s = proper_trajectory(req.samples, "pi")
+            k = _array.to_tensor(s, self.device, torch.float32).reshape(-1, len(shape))
+            plan.setpts(k)
+        self.plan_bytes += plan.device_bytes
+        return key, plan
+
+    def _admit(self):
+        while self.queue and self.free_streams:
+            req = self.queue[0]
+            need = request_bytes(tuple(req.shape), int(np.asarray(req.kspace.shape)[-1]),
+                                 req.n_coils, self.eps)
+            if (self.active or self.finishing) and self.used + need > self.budget:
+                break
+            self.queue.popleft()
+            si = self.free_streams.pop()
+            stream = self.streams[si]
+            key, plan = self._acquire_plan(req, stream)
+            solve = _Solve(self, req, plan, stream)
+            solve.key, solve.si = key, si
+            self.used += solve.bytes
+            req.t_admit = self.now()
+            self.active.append(solve)
+
+    def _retire(self):
+        still = []
+        for s in self.finishing:
+            if s.event.query():
+                s.req.result = s.image
+                s.req.lipschitz = s.L
+                s.req.t_done = self.now()
+                self.used -= s.bytes
+                self.plans[s.key].append(s.plan)
+                self.free_streams.append(s.si)
+                self.done.append(s.req)
+            else:
+                still.append(s)
+        self.finishing = still
+
+    def tick(self):
+        """Admit, issue one unit of every admitted request, retire finished ones."""
+        self._admit()
+        running = []
+        for s in self.active:
+            if s.step():
+                running.append(s)
+            else:
+                self.finishing.append(s)
+        self.active = running
+        self._retire()
+
+    def idle(self):
+        return not (self.queue or self.active or self.finishing)
+
+    def run(self, requests, realtime=True, poll_s=0.0005):
+        """Serve ``requests`` (arrival times in seconds from now when
+        ``realtime``, else all at once) until every one is done."""
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        self.t0 = time.perf_counter()
+        while pending or not self.idle():
+            now = self.now()
+            while pending and (not realtime or pending[0].arrival <= now):
+                self.submit(pending.popleft())
+            if self.idle():
+                if pending:
+                    time.sleep(max(0.0, min(poll_s * 10, pending[0].arrival - now)))
+                continue
+            self.tick()
+            if not self.active and self.finishing:
+                time.sleep(poll_s)
+        torch.cuda.synchronize(self.device)
+        return self.done
+
+    @staticmethod
+    def stats(done, wall_s=None):
+        lat = np.array([(r.t_done - r.arrival) * 1e3 for r in done])
+        t_end = max(r.t_done for r in done)
+        t_begin = min(r.arrival for r in done)
+        wall = wall_s if wall_s is not None else (t_end - t_begin)
+        return {
+            "requests": len(done),
+            "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()),
+            "recon_per_s": len(done) / wall if wall > 0 else float("nan"),
+            "wall_s": wall,
+        }
