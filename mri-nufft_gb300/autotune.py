@@ -22,16 +22,18 @@ from .params import fine_shape
 from .plan import NufftPlan
 
 CANDIDATES = {
+    # "auto" is the dimension's default kernel (2D: warp-cooperative direct
+    # interpolation; 3D: shared-memory tiles); in 2D the bins set the sort
+    # order (locality) of the direct kernels
     2: [
-        {"bins": (32, 32), "interp": "tile", "maxsub": 512},
-        {"bins": (16, 16), "interp": "tile", "maxsub": 512},
-        {"bins": (64, 64), "interp": "tile", "maxsub": 1024},
-        {"bins": (32, 32), "interp": "warp_direct", "maxsub": 512},
-        {"bins": (16, 16), "interp": "direct", "maxsub": 512},
+        {"bins": (32, 32), "interp": "auto", "maxsub": 512},
+        {"bins": (16, 16), "interp": "auto", "maxsub": 512},
+        {"bins": (64, 64), "interp": "auto", "maxsub": 1024},
+        {"bins": (8, 8), "interp": "auto", "maxsub": 512},
     ],
     3: [
-        {"bins": (8, 8, 8), "interp": "tile", "maxsub": 512},
-        {"bins": (9, 9, 9), "interp": "tile", "maxsub": 512},
+        {"bins": (8, 8, 8), "interp": "auto", "maxsub": 512},
+        {"bins": (9, 9, 9), "interp": "auto", "maxsub": 512},
         {"bins": (8, 8, 8), "interp": "warp_direct", "maxsub": 512},
         {"bins": (9, 9, 9), "interp": "warp_direct", "maxsub": 512},
     ],

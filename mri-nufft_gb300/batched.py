@@ -39,9 +39,9 @@ class BatchedNufft:
         self.eps = eps
         self.plans, self.imgs, self.ksps, self.smaps, self.dens = [], [], [], [], []
         self.shapes, self.coils, self.sense, self.scales = [], [], [], []
-        # the batched interp kernel stages tiles: tune bins and subproblem size
+        # the batched kernels are the dimension's defaults: tune bins and subproblem size
         tuner = tuner if tuner is not None else (
-            Autotuner(eps=eps, interp_methods=("tile",)) if autotune else None)
+            Autotuner(eps=eps, interp_methods=("auto",)) if autotune else None)
         dims = set()
         for inst in instances:
             shape = tuple(int(v) for v in inst["shape"])

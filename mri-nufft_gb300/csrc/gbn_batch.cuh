@@ -30,8 +30,8 @@ struct WorkItem {
 struct BatchTables {
   const BatchInst* inst;
   const WorkItem* sub;  int nsub;     // (instance, subproblem)
-  const WorkItem* fblk; int nfblk;    // (instance, block of 256 fine cells)
-  const WorkItem* iblk; int niblk;    // (instance, block of 256 image pixels)
+  const WorkItem* fblk; int nfblk;    // (instance, block of 4096 fine cells)
+  const WorkItem* iblk; int niblk;    // (instance, block of 4096 image pixels)
   const WorkItem* sblk; int nsblk;    // (instance, block of 256 sorted samples)
   int dim;
   int w7;                             // every instance has kernel width 7

@@ -498,7 +498,12 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
                         : std::strcmp(e, "wc") == 0 ? 4
                         : std::strcmp(e, "twc") == 0 ? 5
                                                      : 0;
-    if (const char* e = std::getenv("GBN_SPREAD")) g.method_spread = std::strcmp(e, "gm") == 0;
+    if (const char* e = std::getenv("GBN_INTERP_THREADS")) {
+      int v = std::atoi(e);
+      if (v == 64 || v == 128 || v == 256) g.interp_threads = v;
+    }
+    if (const char* e = std::getenv("GBN_SPREAD"))
+      g.method_spread = std::strcmp(e, "gm") == 0 ? 1 : std::strcmp(e, "wc") == 0 ? 2 : 0;
     for (int d = 0; d < 3; ++d) {
       if (d < dim) {
         int64_t N = n_modes[d];
@@ -964,15 +969,31 @@ int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* ou
 // ----------------------------------------------------------------------------
 // Batches of independent plans
 // ----------------------------------------------------------------------------
+// Instances with the same fine grid share one contiguous pool of fine grids,
+// so that one batched cuFFT call per grid size serves all of them.
+struct FftGroup {
+  int nf[3];
+  int dim;
+  int64_t G;
+  int slots;  // sum of the members' ntrans
+  float2* pool = nullptr;
+  cufftHandle plan = 0;
+};
+
 struct gbn_batch_s {
   std::vector<gbn_plan> plans;
   std::vector<BatchInst> h_inst;
+  std::vector<FftGroup> groups;
   BatchInst* d_inst = nullptr;
   WorkItem* d_work = nullptr;
   BatchTables t{};
   int device = 0;
   bool bound = false;
   ~gbn_batch_s() {
+    for (auto& gr : groups) {
+      if (gr.plan) cufftDestroy(gr.plan);
+      dev_free(gr.pool);
+    }
     dev_free(d_inst);
     dev_free(d_work);
   }
@@ -1014,11 +1035,54 @@ int gbn_batch_create(int n, const gbn_plan* plans, gbn_batch* out) {
       for (int d = 0; d < 3; ++d) bi.dec[d] = p->dec[d];
       b->h_inst.push_back(bi);
       for (int s = 0; s < p->nsub; ++s) sub.push_back({i, s});
-      for (int64_t k = 0; k < (p->g.G + GBN_THREADS - 1) / GBN_THREADS; ++k) fblk.push_back({i, (int)k});
-      for (int64_t k = 0; k < (p->g.Nimg + GBN_THREADS - 1) / GBN_THREADS; ++k) iblk.push_back({i, (int)k});
-      for (int64_t k = 0; k < (p->M + GBN_THREADS - 1) / GBN_THREADS; ++k) sblk.push_back({i, (int)k});
+      const int64_t cblock = (int64_t)GBN_THREADS * 16;  // cells per pad / zero / crop item
+      for (int64_t k = 0; k < (p->g.G + cblock - 1) / cblock; ++k) fblk.push_back({i, (int)k});
+      for (int64_t k = 0; k < (p->g.Nimg + cblock - 1) / cblock; ++k) iblk.push_back({i, (int)k});
+      const int sblock = 256;  // samples per batched sample-block work item
+      for (int64_t k = 0; k < (p->M + sblock - 1) / sblock; ++k) sblk.push_back({i, (int)k});
       size_t tb = (size_t)p->g.tile * sizeof(float2);
       if (tb > tile_bytes) tile_bytes = tb;
+    }
+    // group instances by fine-grid shape; each group gets one pool and one
+    // cuFFT plan over all its coil slots
+    for (int i = 0; i < n; ++i) {
+      gbn_plan p = plans[i];
+      int gi = -1;
+      for (size_t k = 0; k < b->groups.size(); ++k) {
+        const FftGroup& gr = b->groups[k];
+        if (gr.nf[0] == p->g.nf[0] && gr.nf[1] == p->g.nf[1] && gr.nf[2] == p->g.nf[2]) gi = (int)k;
+      }
+      if (gi < 0) {
+        FftGroup gr;
+        for (int d = 0; d < 3; ++d) gr.nf[d] = p->g.nf[d];
+        gr.dim = p->g.dim;
+        gr.G = p->g.G;
+        gr.slots = 0;
+        b->groups.push_back(gr);
+        gi = (int)b->groups.size() - 1;
+      }
+      b->groups[gi].slots += p->ntrans;
+    }
+    for (auto& gr : b->groups) {
+      gr.pool = dev_alloc<float2>((size_t)gr.slots * gr.G, tmp, "batch fine-grid pool");
+      int nn[3] = {gr.nf[0], gr.nf[1], gr.nf[2]};
+      ckfft(cufftPlanMany(&gr.plan, gr.dim, nn, nullptr, 1, (int)gr.G, nullptr, 1, (int)gr.G,
+                          CUFFT_C2C, gr.slots),
+            "cufftPlanMany");
+    }
+    {
+      std::vector<int> used(b->groups.size(), 0);
+      for (int i = 0; i < n; ++i) {
+        gbn_plan p = plans[i];
+        for (size_t k = 0; k < b->groups.size(); ++k) {
+          FftGroup& gr = b->groups[k];
+          if (gr.nf[0] == p->g.nf[0] && gr.nf[1] == p->g.nf[1] && gr.nf[2] == p->g.nf[2]) {
+            b->h_inst[i].fine = gr.pool + (int64_t)used[k] * gr.G;
+            used[k] += p->ntrans;
+            break;
+          }
+        }
+      }
     }
     std::vector<WorkItem> all;
     all.insert(all.end(), sub.begin(), sub.end());
@@ -1103,16 +1167,22 @@ static int batch_run(gbn_batch b, bool adjoint, gbn_stream stream) {
   try {
     DeviceGuard dg(b->device);
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    auto ffts = [&](int dir) {
+      for (auto& gr : b->groups) {
+        ckfft(cufftSetStream(gr.plan, st), "cufftSetStream");
+        ckfft(cufftExecC2C(gr.plan, reinterpret_cast<cufftComplex*>(gr.pool),
+                           reinterpret_cast<cufftComplex*>(gr.pool), dir),
+              "cufftExecC2C");
+      }
+    };
     if (!adjoint) {
       ck(batch_pad(b->t, st), "batch pad");
-      for (size_t i = 0; i < b->plans.size(); ++i)
-        b->plans[i]->exec_fft(b->h_inst[i].ncoils, b->plans[i]->fine, -1, st);
+      ffts(CUFFT_FORWARD);
       ck(batch_interp(b->t, st), "batch interp");
     } else {
       ck(batch_zero(b->t, st), "batch zero");
       ck(batch_spread(b->t, st), "batch spread");
-      for (size_t i = 0; i < b->plans.size(); ++i)
-        b->plans[i]->exec_fft(b->h_inst[i].ncoils, b->plans[i]->fine, +1, st);
+      ffts(CUFFT_INVERSE);
       ck(batch_crop(b->t, st), "batch crop");
     }
     return GBN_OK;

@@ -38,7 +38,8 @@ struct Geom {
   int tile;      // padded tile cells = prod(pd)
   int interp_cg; // coils per interp tile pass (0: automatic)
   int method_interp;  // 0: tiles, 1: direct from the fine grid, 3: double-buffered tiles
-  int method_spread;  // 0: automatic, 1: global atomics
+  int method_spread;  // 0: automatic, 1: global atomics, 2: warp-cooperative atomics
+  int interp_threads; // CTA size of the tile interp kernel (0: 128)
 };
 
 // Work table of one sorted trajectory.

@@ -82,7 +82,9 @@ class NufftPlan:
         return b.value
 
     # ---------------------------------------------------------------- tuning
-    METHODS = {"tile": 0, "direct": 1, "double_buffered": 3, "warp_direct": 4, "warp_tile": 5}
+    # "auto": the default kernel of the dimension (2D: warp-cooperative direct,
+    # 3D: shared-memory tiles)
+    METHODS = {"auto": 0, "direct": 1, "double_buffered": 3, "warp_direct": 4, "warp_tile": 5}
 
     def tune(self, bins=None, interp=None, maxsub_cap=0):
         """Set bin sizes (fine cells per axis), interpolation method and the

@@ -45,7 +45,7 @@ def test_batched_equals_single(gpu_pkg, tmp_path, dim):
 
     rng = np.random.default_rng(dim)
     insts = _instances(rng, dim)
-    tuner = Autotuner(cache_path=tmp_path / "tune.json", interp_methods=("tile",))
+    tuner = Autotuner(cache_path=tmp_path / "tune.json", interp_methods=("auto",))
     bat = BatchedNufft(insts, tuner=tuner)
     assert (tmp_path / "tune.json").exists()
     imgs = [(rng.standard_normal(i["shape"]) + 1j * rng.standard_normal(i["shape"])).astype(np.complex64)
@@ -68,7 +68,7 @@ def test_batched_graph_replay(gpu_pkg, tmp_path):
 
     rng = np.random.default_rng(11)
     insts = _instances(rng, 2)
-    bat = BatchedNufft(insts, tuner=Autotuner(cache_path=tmp_path / "t.json", interp_methods=("tile",)))
+    bat = BatchedNufft(insts, tuner=Autotuner(cache_path=tmp_path / "t.json", interp_methods=("auto",)))
     imgs = [(rng.standard_normal(i["shape"]) + 1j * rng.standard_normal(i["shape"])).astype(np.complex64)
             for i in insts]
     bat.set_images(imgs)
