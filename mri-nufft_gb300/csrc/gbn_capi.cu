@@ -194,11 +194,25 @@ struct gbn_plan_s {
 
   // sort state
   int64_t M = -1, Mcap = 0, subcap = 0;
+  int64_t point_bytes = 0;  // device bytes of the per-point arrays
   int maxsub = 256;
   int maxsub_cap = 512;
   int nsub = 0;
   SortBuffers sb{};
-  int nbins = 0;
+  int nbins = 0;           // bins of the sort
+  int64_t bin_bytes = 0;   // device bytes of the per-bin arrays
+
+  // 3D column streaming: the sort is keyed on (x bin, y bin, z cell); the
+  // interp / grad table groups bs2 consecutive z cells (the bins of g), the
+  // spread table cuts each column into chunks of <= kStreamChunk samples
+  int stream_spread = 0;
+  int ngrp = 0;            // interp groups (bins of g)
+  int ncol = 0;            // columns
+  int* grp = nullptr;      // group-table scratch, 4 x (ngrp + ncol)
+  int* ssub = nullptr;     // spread chunk table, 3 x sscap
+  int64_t sscap = 0;
+  int nsub_s = 0;
+  int maxsub_s = 0;
 
   std::map<int, cufftHandle> ffts;
 
@@ -226,12 +240,37 @@ struct gbn_plan_s {
     dev_free(fine);
     dev_free(kbuf);
     free_points();
+    free_bins();
+    dev_free(sb.d_total);
+  }
+
+  void free_bins() {
     dev_free(sb.bin_count);
     dev_free(sb.bin_start);
     dev_free(sb.nsub_bin);
     dev_free(sb.sub_off);
     dev_free(sb.scan_scratch);
-    dev_free(sb.d_total);
+    dev_free(grp);
+    sb.bin_count = sb.bin_start = sb.nsub_bin = sb.sub_off = sb.scan_scratch = grp = nullptr;
+    bytes -= bin_bytes;
+    bin_bytes = 0;
+  }
+
+  // (Re)allocates the per-bin arrays for the current geometry.
+  void setup_bins() {
+    free_bins();
+    stream_spread = stream_fit(g) ? 1 : 0;
+    ngrp = g.nb[0] * g.nb[1] * g.nb[2];
+    ncol = g.nb[0] * g.nb[1];
+    nbins = stream_spread ? ncol * g.nf[2] : ngrp;
+    const int64_t b0 = bytes;
+    sb.bin_count = dev_alloc<int>(nbins, bytes, "bins");
+    sb.bin_start = dev_alloc<int>(nbins, bytes, "bins");
+    sb.nsub_bin = dev_alloc<int>(nbins, bytes, "bins");
+    sb.sub_off = dev_alloc<int>(nbins, bytes, "bins");
+    sb.scan_scratch = dev_alloc<int>(scan_scratch_ints(nbins), bytes, "scan");
+    if (stream_spread) grp = dev_alloc<int>(4 * ((size_t)ngrp + ncol), bytes, "bin groups");
+    bin_bytes = bytes - b0;
   }
 
   void free_points() {
@@ -242,6 +281,9 @@ struct gbn_plan_s {
     dev_free(sb.sub_bin);
     dev_free(sb.sub_start);
     dev_free(sb.sub_count);
+    dev_free(ssub);
+    ssub = nullptr;
+    sscap = 0;
     sb.bin_of = sb.rank_of = sb.perm = sb.sub_bin = sb.sub_start = sb.sub_count = nullptr;
     sb.u[0] = sb.u[1] = sb.u[2] = nullptr;
   }
@@ -256,6 +298,19 @@ struct gbn_plan_s {
     s.sub_count = sb.sub_count;
     s.nsub = nsub;
     s.maxsub = maxsub;
+    return s;
+  }
+
+  // the table the spreader walks: column chunks when streaming
+  Sorted sorted_spread() const {
+    Sorted s = sorted();
+    if (stream_spread) {
+      s.sub_bin = ssub;
+      s.sub_start = ssub + sscap;
+      s.sub_count = ssub + 2 * sscap;
+      s.nsub = nsub_s;
+      s.maxsub = maxsub_s;
+    }
     return s;
   }
 
@@ -321,7 +376,10 @@ void run_interp(gbn_plan p, const InterpArgs& a, cudaStream_t st) {
 void run_spread(gbn_plan p, const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return;
   Span span(p, GBN_STAGE_SPREAD, st);
-  ck(a.g.dim == 2 ? launch_spread2d(a, st) : launch_spread3d(a, st), "spread kernel");
+  ck(a.g.dim == 2        ? launch_spread2d(a, st)
+     : p->stream_spread ? launch_spread_stream3d(a, st)
+                        : launch_spread3d(a, st),
+     "spread kernel");
   p->launches++;
 }
 void run_pad(gbn_plan p, const PadArgs& a, cudaStream_t st) {
@@ -389,7 +447,7 @@ SpreadArgs spread_args(gbn_plan p, const float2* in, const float* density, float
                        int ntr, float scale) {
   SpreadArgs a{};
   a.g = p->g;
-  a.s = p->sorted();
+  a.s = p->sorted_spread();
   a.in = in;
   a.density = density;
   a.fine = fine;
@@ -492,6 +550,7 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
           if (v[d] >= 1 && v[d] <= 64) (dim == 2 ? binsz2[d] : binsz3[d]) = v[d];
     }
     if (const char* e = std::getenv("GBN_INTERP_CG")) g.interp_cg = std::atoi(e);
+    if (const char* e = std::getenv("GBN_SPREAD_CG")) g.spread_cg = std::atoi(e);
     if (const char* e = std::getenv("GBN_INTERP"))
       g.method_interp = std::strcmp(e, "gm") == 0   ? 1
                         : std::strcmp(e, "db") == 0 ? 3
@@ -503,7 +562,11 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
       if (v == 64 || v == 128 || v == 256) g.interp_threads = v;
     }
     if (const char* e = std::getenv("GBN_SPREAD"))
-      g.method_spread = std::strcmp(e, "gm") == 0 ? 1 : std::strcmp(e, "wc") == 0 ? 2 : 0;
+      g.method_spread = std::strcmp(e, "gm") == 0       ? 1
+                        : std::strcmp(e, "wc") == 0     ? 2
+                        : std::strcmp(e, "stream") == 0 ? 3
+                        : std::strcmp(e, "rows") == 0   ? 4
+                                                        : 0;
     for (int d = 0; d < 3; ++d) {
       if (d < dim) {
         int64_t N = n_modes[d];
@@ -533,8 +596,6 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
     if (g.G > ((int64_t)1 << 31) - 1) fail(GBN_ERR_ARG, "fine grid larger than 2^31 cells");
     g.tile = g.pd[0] * g.pd[1] * g.pd[2];
     if ((int64_t)g.tile * 8 > kTileSmemBudget) fail(GBN_ERR_ARG, "tile does not fit shared memory");
-    p->nbins = g.nb[0] * g.nb[1] * g.nb[2];
-
     if (!spread_only) {
       for (int d = 0; d < dim; ++d) {
         std::vector<float> f = deconv_factors(g.n[d], g.nf[d], w, beta);
@@ -544,12 +605,8 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
       }
     }
     p->fine = dev_alloc<float2>((size_t)ntrans * g.G, p->bytes, "fine grid");
-    p->sb.bin_count = dev_alloc<int>(p->nbins, p->bytes, "bins");
-    p->sb.bin_start = dev_alloc<int>(p->nbins, p->bytes, "bins");
-    p->sb.nsub_bin = dev_alloc<int>(p->nbins, p->bytes, "bins");
-    p->sb.sub_off = dev_alloc<int>(p->nbins, p->bytes, "bins");
-    p->sb.scan_scratch = dev_alloc<int>(scan_scratch_ints(p->nbins), p->bytes, "scan");
-    p->sb.d_total = dev_alloc<int>(1, p->bytes, "scan");
+    p->setup_bins();
+    p->sb.d_total = dev_alloc<int>(2, p->bytes, "scan");
     *out = p;
     return GBN_OK;
   } catch (const Fail& e) {
@@ -611,15 +668,20 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
     }
     int maxsub = 32;
     while (maxsub < target && maxsub < cap) maxsub <<= 1;
-    int64_t subcap = M / maxsub + (M < p->nbins ? M : p->nbins) + 1;
-    if (M > p->Mcap || subcap > p->subcap) {
+    int64_t subcap = M / maxsub + (M < p->ngrp ? M : p->ngrp) + 1;
+    // spread chunks of the streaming kernel: one CTA batch at most
+    const int maxsub_s = maxsub < kStreamChunk ? maxsub : kStreamChunk;
+    int64_t sscap = p->stream_spread ? M / maxsub_s + (M < p->ncol ? M : p->ncol) + 1 : 0;
+    if (M > p->Mcap || subcap > p->subcap || sscap > p->sscap) {
       // free the previous point buffers before the new ones (bytes tally)
-      int64_t old = 0;
-      if (p->sb.perm) old = p->Mcap * (int64_t)(4 * 3 + 4 * p->g.dim) + p->subcap * 12;
-      p->free_points();
-      p->bytes -= old;
       int64_t cap = M > p->Mcap ? M : p->Mcap;
       int64_t scap = subcap > p->subcap ? subcap : p->subcap;
+      int64_t sscap2 = sscap > p->sscap ? sscap : p->sscap;
+      p->free_points();
+      p->bytes -= p->point_bytes;
+      p->point_bytes = 0;
+      p->Mcap = p->subcap = p->sscap = 0;
+      const int64_t b0 = p->bytes;
       p->sb.bin_of = dev_alloc<int>(cap, p->bytes, "sort scratch");
       p->sb.rank_of = dev_alloc<int>(cap, p->bytes, "sort scratch");
       p->sb.perm = dev_alloc<int>(cap, p->bytes, "permutation");
@@ -627,17 +689,42 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
       p->sb.sub_bin = dev_alloc<int>(scap, p->bytes, "subproblems");
       p->sb.sub_start = dev_alloc<int>(scap, p->bytes, "subproblems");
       p->sb.sub_count = dev_alloc<int>(scap, p->bytes, "subproblems");
+      if (sscap2 > 0) p->ssub = dev_alloc<int>(3 * sscap2, p->bytes, "spread chunks");
+      p->point_bytes = p->bytes - b0;
       p->Mcap = cap;
       p->subcap = scap;
+      p->sscap = sscap2;
     }
     const float* k[3] = {k0, k1, k2};
     p->maxsub = maxsub;
-    ck(sort_points(p->g, M, k, maxsub, p->sb, st), "sort");
-    int total = 0;
-    ck(cudaMemcpyAsync(&total, p->sb.d_total, sizeof(int), cudaMemcpyDeviceToHost, st),
+    p->maxsub_s = maxsub_s;
+    int totals[2] = {0, 0};
+    if (p->stream_spread) {
+      const Geom& g = p->g;
+      Geom gs = g;  // sort key (x bin, y bin, z cell)
+      gs.bs[2] = 1;
+      gs.nb[2] = g.nf[2];
+      ck(sort_points(gs, M, k, maxsub, p->sb, st, false), "sort");
+      int* q = p->grp;
+      GroupBuffers gi{q, q + p->ngrp, q + 2 * p->ngrp, q + 3 * p->ngrp,
+                      p->sb.sub_bin, p->sb.sub_start, p->sb.sub_count};
+      q += 4 * (size_t)p->ngrp;
+      GroupBuffers gc{q, q + p->ncol, q + 2 * p->ncol, q + 3 * p->ncol,
+                      p->ssub, p->ssub + p->sscap, p->ssub + 2 * p->sscap};
+      ck(build_group_table(p->ngrp, g.nb[2], g.bs[2], g.nf[2], maxsub, p->sb, gi, p->sb.d_total, st),
+         "interp groups");
+      ck(build_group_table(p->ncol, 1, g.nf[2], g.nf[2], maxsub_s, p->sb, gc, p->sb.d_total + 1, st),
+         "spread chunks");
+    } else {
+      ck(sort_points(p->g, M, k, maxsub, p->sb, st, true), "sort");
+    }
+    ck(cudaMemcpyAsync(totals, p->sb.d_total, sizeof(totals), cudaMemcpyDeviceToHost, st),
        "copy subproblem count");
     ck(cudaStreamSynchronize(st), "setpts sync");
-    if (total > p->subcap) fail(GBN_ERR_CUDA, "subproblem table overflow");
+    const int total = totals[0];
+    if (total > p->subcap || (p->stream_spread && totals[1] > p->sscap))
+      fail(GBN_ERR_CUDA, "subproblem table overflow");
+    p->nsub_s = p->stream_spread ? totals[1] : 0;
     p->nsub = total;
     p->M = M;
   });
@@ -861,23 +948,8 @@ int gbn_plan_tune(gbn_plan p, const int* bins, int interp_method, int maxsub_cap
       }
       t.tile = t.pd[0] * t.pd[1] * t.pd[2];
       if ((int64_t)t.tile * 8 > kTileSmemBudget) fail(GBN_ERR_ARG, "tile does not fit shared memory");
-      const int nbins = t.nb[0] * t.nb[1] * t.nb[2];
-      if (nbins != p->nbins) {
-        dev_free(p->sb.bin_count);
-        dev_free(p->sb.bin_start);
-        dev_free(p->sb.nsub_bin);
-        dev_free(p->sb.sub_off);
-        dev_free(p->sb.scan_scratch);
-        p->bytes -= (int64_t)p->nbins * 16 + (int64_t)scan_scratch_ints(p->nbins) * 4;
-        p->sb.bin_count = p->sb.bin_start = p->sb.nsub_bin = p->sb.sub_off = p->sb.scan_scratch = nullptr;
-        p->nbins = nbins;
-        p->sb.bin_count = dev_alloc<int>(nbins, p->bytes, "bins");
-        p->sb.bin_start = dev_alloc<int>(nbins, p->bytes, "bins");
-        p->sb.nsub_bin = dev_alloc<int>(nbins, p->bytes, "bins");
-        p->sb.sub_off = dev_alloc<int>(nbins, p->bytes, "bins");
-        p->sb.scan_scratch = dev_alloc<int>(scan_scratch_ints(nbins), p->bytes, "scan");
-      }
       g = t;
+      p->setup_bins();
       p->M = -1;  // points must be set again
     }
     if (interp_method >= 0) {

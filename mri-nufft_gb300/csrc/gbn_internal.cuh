@@ -38,8 +38,10 @@ struct Geom {
   int tile;      // padded tile cells = prod(pd)
   int interp_cg; // coils per interp tile pass (0: automatic)
   int method_interp;  // 0: tiles, 1: direct from the fine grid, 3: double-buffered tiles
-  int method_spread;  // 0: automatic, 1: global atomics, 2: warp-cooperative atomics
+  int method_spread;  // 0: automatic, 1: global atomics, 2: warp-cooperative atomics,
+                      // 3: 3D column streaming, 4: 3D bin-tile rows
   int interp_threads; // CTA size of the tile interp kernel (0: 128)
+  int spread_cg;      // coils per pass of the streaming spreader (0: automatic)
 };
 
 // Work table of one sorted trajectory.
@@ -147,6 +149,8 @@ cudaError_t launch_interp2d(const InterpArgs& a, cudaStream_t st);
 cudaError_t launch_interp3d(const InterpArgs& a, cudaStream_t st);
 cudaError_t launch_spread2d(const SpreadArgs& a, cudaStream_t st);
 cudaError_t launch_spread3d(const SpreadArgs& a, cudaStream_t st);
+// 3D column-streaming spreader; a.s is the column-chunk table
+cudaError_t launch_spread_stream3d(const SpreadArgs& a, cudaStream_t st);
 cudaError_t launch_grad2d(const GradArgs& a, cudaStream_t st);
 cudaError_t launch_grad3d(const GradArgs& a, cudaStream_t st);
 
@@ -167,5 +171,16 @@ inline int coils_per_pass(const Geom& g, int ntr) {
 inline bool rows_fit(const Geom& g) {
   return g.dim == 3 && g.w <= 8 && g.pd[0] <= 16 && g.pd[1] <= 16 && g.pd[2] <= 16;
 }
+
+// 3D widths up to 7 with tile cross-sections up to 16 x 16 rows (and a z
+// extent that fits the kernel's 16-bit sample header) use the
+// column-streaming spreader (an 8-cell register window along z).
+inline bool stream_fit(const Geom& g) {
+  return g.dim == 3 && g.w <= 7 && g.bs[0] <= 15 && g.bs[1] <= 15 && g.pd[0] <= 16 &&
+         g.pd[1] <= 16 && g.nf[2] <= 32768 && (g.method_spread == 0 || g.method_spread == 3);
+}
+
+// Samples per chunk of the column-streaming spreader.
+constexpr int kStreamChunk = 512;
 
 }  // namespace gbn

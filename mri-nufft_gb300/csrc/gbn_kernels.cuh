@@ -820,6 +820,197 @@ spread_rows3d_kernel(SpreadArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Spreading, 3D column-streaming kernel (widths w <= 7).
+//
+// With the sort keyed on (x bin, y bin, z cell), the samples of one column
+// of bins (bs0 x bs1 cells across, the whole z extent) arrive in z order.  A
+// CTA takes a chunk of <= kStreamBatch consecutive samples of one column.
+// Thread t owns row (i0, i1) of the column's padded (bs0 + w) x (bs1 + w)
+// cross-section (two i0 rows per warp, as in the row kernel) and keeps a
+// window of 8 z cells in registers: cell z lives in slot z & 7.  A sample in
+// z cell f covers cells [f - w/2, f - w/2 + 7], so the window is anchored at
+// zb = f - floor(w/2); when the samples reach a later anchor, the slots whose
+// cells fall out of the window are added to the fine grid (float2 global
+// atomics) and cleared.  Each sample's z weights are staged already rotated
+// into slot order, so the accumulation indexes registers statically.
+// Against the bin-tile row kernel each sample updates 8 register cells per
+// coil instead of 16, the kernel weights are evaluated once per chunk for all
+// coils, and a fine cell is flushed once per chunk rather than once per
+// overlapping tile.
+// ---------------------------------------------------------------------------
+constexpr int kStreamBatch = kStreamChunk;
+
+// dynamic shared memory of the streaming kernel for CG coils per pass
+__host__ __device__ constexpr size_t stream_smem_bytes(int cg) {
+  return (size_t)kStreamBatch * (sizeof(unsigned) + 24 * sizeof(float)) +
+         (size_t)cg * kStreamBatch * sizeof(float2);
+}
+
+__device__ __forceinline__ int wrap_near(int i, int n) {
+  // one period of correction covers every window cell when n >= 8; the
+  // modulo keeps tiny grids correct
+  int m = i < 0 ? i + n : (i >= n ? i - n : i);
+  return (unsigned)m < (unsigned)n ? m : wrap_idx(i, n);
+}
+
+// Adds window slot K (fine cell z) of every coil to the fine grid and clears it.
+template <int K, int CG>
+__device__ __forceinline__ void stream_flush(float (&ar)[CG][8], float (&ai)[CG][8], bool own,
+                                             float2* fb, int z, int nf2, int G, int nc) {
+  if (own) {
+    float2* dst = fb + wrap_near(z, nf2);
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc) {
+      if (cc < nc && (ar[cc][K] != 0.f || ai[cc][K] != 0.f))
+        atomicAdd(dst, make_float2(ar[cc][K], ai[cc][K]));
+      dst += G;
+    }
+  }
+#pragma unroll
+  for (int cc = 0; cc < CG; ++cc) ar[cc][K] = ai[cc][K] = 0.f;
+}
+
+// Flushes the window slots set in `mask` (slot k holds cell zb + ((k - zb) & 7)).
+template <int CG>
+__device__ __forceinline__ void stream_flush_mask(unsigned mask, int zb, float (&ar)[CG][8],
+                                                  float (&ai)[CG][8], bool own, float2* fb,
+                                                  int nf2, int G, int nc) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (mask & (1u << k)) {
+      const int z = zb + ((k - zb) & 7);
+      if (k == 0) stream_flush<0, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 1) stream_flush<1, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 2) stream_flush<2, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 3) stream_flush<3, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 4) stream_flush<4, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 5) stream_flush<5, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 6) stream_flush<6, CG>(ar, ai, own, fb, z, nf2, G, nc);
+      if (k == 7) stream_flush<7, CG>(ar, ai, own, fb, z, nf2, G, nc);
+    }
+  }
+}
+
+template <int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS, 2)
+spread_stream3d_kernel(SpreadArgs a) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  float* s_w2 = reinterpret_cast<float*>(s_raw);           // [kStreamBatch][8], slot order
+  float* s_w0 = s_w2 + kStreamBatch * 8;                    // [kStreamBatch][8]
+  float* s_w1 = s_w0 + kStreamBatch * 8;                    // [kStreamBatch][8]
+  float2* s_c = reinterpret_cast<float2*>(s_w1 + kStreamBatch * 8);  // [CG][kStreamBatch]
+  // per sample: window anchor + 8 (bits 0-15), local row offsets a0, a1
+  // (bits 16-19, 20-23), mask of the warps whose rows it covers (bits 24-31)
+  unsigned* s_hd = reinterpret_cast<unsigned*>(s_c + CG * kStreamBatch);
+
+  const Geom& g = a.g;
+  const int sub = blockIdx.x;
+  const int col = a.s.sub_bin[sub];
+  const int p0 = a.s.sub_start[sub];
+  const int cnt = imin(a.s.sub_count[sub], kStreamBatch);
+  const int w = W > 0 ? W : g.w;
+  const int hw = w >> 1;
+  const int o0 = (col / g.nb[1]) * g.bs[0] - hw;
+  const int o1 = (col % g.nb[1]) * g.bs[1] - hw;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // warp w owns rows i0 = 2w, 2w+1 (16 lanes each along i1)
+  const int i0 = 2 * warp + (lane >> 4);
+  const int i1 = lane & 15;
+  const bool own = i0 < g.pd[0] && i1 < g.pd[1];
+  const int nf2 = g.nf[2];
+  // fine grids hold < 2^31 cells
+  const int G = (int)g.G;
+  const int rowbase = own ? (wrap_idx(o0 + i0, g.nf[0]) * g.nf[1] + wrap_idx(o1 + i1, g.nf[1])) * nf2 : 0;
+
+  // geometry of the chunk, once for every coil
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int pos = p0 + t;
+    float wt[WidthTraits<W>::WM];
+    const int a0 = weights_rt<W>(a.s.u[0][pos], g, wt) - o0;  // 0 .. bs0
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s_w0[t * 8 + k] = k < w ? wt[k] : 0.f;
+    const int a1 = weights_rt<W>(a.s.u[1][pos], g, wt) - o1;  // 0 .. bs1
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s_w1[t * 8 + k] = k < w ? wt[k] : 0.f;
+    const float u2 = a.s.u[2][pos];
+    const int zs = cell_of(u2, nf2) - hw;
+    const int off = weights_rt<W>(u2, g, wt) - zs;  // 0 or 1
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int m = k - off;
+      float v = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < WidthTraits<W>::WM; ++kk)
+        if (kk == m && kk < w) v = wt[kk];
+      s_w2[t * 8 + ((zs + k) & 7)] = v;
+    }
+    unsigned wm = 0;
+#pragma unroll
+    for (int q = 0; q < GBN_THREADS / 32; ++q)
+      if (a0 <= 2 * q + 1 && a0 + w > 2 * q) wm |= 1u << q;
+    s_hd[t] = (unsigned)(zs + 8) | ((unsigned)a0 << 16) | ((unsigned)a1 << 20) | (wm << 24);
+  }
+
+  const unsigned mybit = 1u << (24 + warp);
+  for (int c0 = 0; c0 < a.ntr; c0 += CG) {
+    const int nc = imin(CG, a.ntr - c0);
+    // strengths of this pass's coils
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+      const int j = a.s.perm[p0 + t];
+      float dj = a.scale;
+      if (a.density) dj *= a.density[j];
+#pragma unroll
+      for (int cc = 0; cc < CG; ++cc) {
+        float2 x = cc < nc ? a.in[(int64_t)(c0 + cc) * a.s.M + j] : make_float2(0.f, 0.f);
+        s_c[cc * kStreamBatch + t] = make_float2(x.x * dj, x.y * dj);
+      }
+    }
+    __syncthreads();
+    float ar[CG][8], ai[CG][8];
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+    float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
+    int zb = cnt > 0 ? (int)(s_hd[0] & 0xffffu) - 8 : 0;  // window: cells zb .. zb + 7
+
+#pragma unroll 1
+    for (int s = 0; s < cnt; ++s) {
+      const unsigned hd = s_hd[s];
+      const int zs = (int)(hd & 0xffffu) - 8;
+      if (zs != zb) {  // the same for every thread: flush the cells that leave the window
+        const int steps = imin(zs - zb, 8);
+        const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
+        stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf2, G, nc);
+        zb = zs;
+      }
+      if (hd & mybit) {  // warp-uniform
+        const unsigned r0 = (unsigned)(i0 - (int)((hd >> 16) & 15u));
+        const unsigned r1 = (unsigned)(i1 - (int)((hd >> 20) & 15u));
+        if (own && r0 < (unsigned)w && r1 < (unsigned)w) {
+          const float kw = s_w0[s * 8 + r0] * s_w1[s * 8 + r1];
+          const float4* w4 = reinterpret_cast<const float4*>(s_w2 + s * 8);
+          const float4 wa = w4[0], wb = w4[1];
+          const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+          for (int cc = 0; cc < CG; ++cc) {
+            const float2 c = s_c[cc * kStreamBatch + s];
+            const float vr = kw * c.x, vi = kw * c.y;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
+              ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
+            }
+          }
+        }
+      }
+    }
+    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf2, G, nc);
+    __syncthreads();  // s_c is restaged by the next pass
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Spreading, sample-driven kernel with global vector atomics (2D, and any
 // width the row kernel does not cover).  Threads take consecutive sorted
 // samples, so the float2 reductions of a warp land on nearby cells of the
@@ -1043,6 +1234,29 @@ cudaError_t launch_spread_rows_t(const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return cudaSuccess;
   spread_rows3d_kernel<W, CG><<<a.s.nsub, GBN_THREADS, 0, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int W, int CG>
+cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return cudaSuccess;
+  const size_t smem = stream_smem_bytes(CG);
+  auto k = spread_stream3d_kernel<W, CG>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.s.nsub, GBN_THREADS, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// a.s is the column-chunk table (sub_bin = column index)
+inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st) {
+  int cg = a.ntr >= 3 ? 4 : a.ntr;
+  if (a.g.spread_cg == 1 || a.g.spread_cg == 2 || a.g.spread_cg == 4) cg = imin(cg, a.g.spread_cg);
+  if (a.g.w == 7) {
+    if (cg == 4) return launch_spread_stream_t<7, 4>(a, st);
+    return cg == 2 ? launch_spread_stream_t<7, 2>(a, st) : launch_spread_stream_t<7, 1>(a, st);
+  }
+  if (cg == 4) return launch_spread_stream_t<0, 4>(a, st);
+  return cg == 2 ? launch_spread_stream_t<0, 2>(a, st) : launch_spread_stream_t<0, 1>(a, st);
 }
 
 template <int DIM, int W>

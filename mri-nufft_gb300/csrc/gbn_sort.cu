@@ -77,6 +77,24 @@ __global__ void fill_sub_kernel(int nbins, const int* __restrict__ bin_count,
   }
 }
 
+// Groups of K consecutive bins along the last axis (bins of one column are
+// contiguous in the sorted order): group gi = column * ngz + gz covers the
+// bins of layers [gz*K, min(nl, gz*K + K)) of its column.
+__global__ void group_kernel(int ngroups, int ngz, int K, int nl, const int* __restrict__ bin_count,
+                             const int* __restrict__ bin_start, int* __restrict__ grp_count,
+                             int* __restrict__ grp_start) {
+  int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= ngroups) return;
+  const int col = gi / ngz, gz = gi - col * ngz;
+  const int l0 = gz * K;
+  const int l1 = imin(nl, l0 + K);
+  const int64_t b = (int64_t)col * nl;
+  int c = 0;
+  for (int l = l0; l < l1; ++l) c += bin_count[b + l];
+  grp_count[gi] = c;
+  grp_start[gi] = bin_start[b + l0];
+}
+
 // ---------------------------------------------------------------------------
 // Exclusive scan of int arrays (block scan + scan of block sums + add).
 // ---------------------------------------------------------------------------
@@ -170,8 +188,22 @@ cudaError_t exclusive_scan(const int* in, int* out, int n, int* scratch, int* to
   return cudaGetLastError();
 }
 
+cudaError_t build_group_table(int ngroups, int ngz, int K, int nl, int maxsub,
+                              const SortBuffers& sb, const GroupBuffers& gb, int* d_total,
+                              cudaStream_t st) {
+  int bb = (ngroups + 255) / 256;
+  group_kernel<<<bb, 256, 0, st>>>(ngroups, ngz, K, nl, sb.bin_count, sb.bin_start, gb.grp_count,
+                                   gb.grp_start);
+  nsub_kernel<<<bb, 256, 0, st>>>(ngroups, gb.grp_count, maxsub, gb.nsub_grp);
+  cudaError_t e = exclusive_scan(gb.nsub_grp, gb.grp_off, ngroups, sb.scan_scratch, d_total, st);
+  if (e != cudaSuccess) return e;
+  fill_sub_kernel<<<bb, 256, 0, st>>>(ngroups, gb.grp_count, gb.grp_start, gb.grp_off, maxsub,
+                                      gb.sub_bin, gb.sub_start, gb.sub_count);
+  return cudaGetLastError();
+}
+
 cudaError_t sort_points(const Geom& g, int64_t M, const float* const k[3], int maxsub,
-                        const SortBuffers& sb, cudaStream_t st) {
+                        const SortBuffers& sb, cudaStream_t st, bool subproblems) {
   const int nbins = g.nb[0] * g.nb[1] * g.nb[2];
   cudaError_t e = cudaMemsetAsync(sb.bin_count, 0, sizeof(int) * nbins, st);
   if (e != cudaSuccess) return e;
@@ -188,6 +220,7 @@ cudaError_t sort_points(const Geom& g, int64_t M, const float* const k[3], int m
     scatter_kernel<<<blocks, 256, 0, st>>>(g, M, k[0], k[1], k2, sb.bin_of, sb.rank_of,
                                            sb.bin_start, sb.perm, sb.u[0], sb.u[1], sb.u[2]);
   }
+  if (!subproblems) return cudaGetLastError();
   int bb = (nbins + 255) / 256;
   nsub_kernel<<<bb, 256, 0, st>>>(nbins, sb.bin_count, maxsub, sb.nsub_bin);
   e = exclusive_scan(sb.nsub_bin, sb.sub_off, nbins, sb.scan_scratch, sb.d_total, st);

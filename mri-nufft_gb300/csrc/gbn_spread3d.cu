@@ -3,4 +3,7 @@
 
 namespace gbn {
 cudaError_t launch_spread3d(const SpreadArgs& a, cudaStream_t st) { return dispatch_spread<3>(a, st); }
+cudaError_t launch_spread_stream3d(const SpreadArgs& a, cudaStream_t st) {
+  return dispatch_spread_stream3d(a, st);
+}
 }  // namespace gbn

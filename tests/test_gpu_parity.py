@@ -106,6 +106,29 @@ def test_3d_multicoil_kooshball_subset(gpu_pkg, pkg):
     assert rel_l2(x[vox], ref) < TOL
 
 
+@pytest.mark.parametrize("eps,tol", [(1e-6, 1e-4), (1e-3, 5e-3)])
+@pytest.mark.parametrize("C", [1, 2, 3, 5])
+def test_3d_dense_columns_coil_counts(gpu_pkg, eps, tol, C):
+    # 3D adjoint with samples packed into a few columns of the fine grid (many
+    # spread chunks per column, long z runs), for every coils-per-pass count
+    # and both the fixed-width and the generic-width kernels
+    rng = np.random.default_rng(13)
+    shape = (24, 20, 28)
+    M = 30000
+    s = np.clip(rng.normal(0.0, 0.08, (M, 3)), -0.5, 0.4999)
+    s[: M // 3, 2] = rng.uniform(-0.5, 0.5, M // 3)
+    s[:2] = [[-0.5, -0.5, -0.5], [0.4999, 0.4999, 0.4999]]
+    s = s.astype(np.float32)
+    ksp = (rng.standard_normal((C, M)) + 1j * rng.standard_normal((C, M))).astype(np.complex64)
+    op = gpu_pkg.MRIGB300(s, shape, n_coils=C, eps=eps)
+    x = op.adj_op(ksp).reshape(C, -1)
+    vox = rng.choice(int(np.prod(shape)), 200, replace=False)
+    nf = ndft.norm_factor(shape)
+    for c in range(C):
+        ref = ndft.ndft_type1_voxels(s, ksp[c], shape, vox) / nf
+        assert rel_l2(x[c, vox], ref) < tol
+
+
 def test_density_and_boundaries(gpu_pkg):
     rng = np.random.default_rng(7)
     shape = (32, 32)
