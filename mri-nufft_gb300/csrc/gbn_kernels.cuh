@@ -92,24 +92,60 @@ __device__ __forceinline__ int64_t tile_to_fine(const Geom& g, const int* o, int
   }
 }
 
+// Largest number of tile rows (all axes but the last) whose fine-grid offsets
+// are tabulated in shared memory; larger tiles compute them per load.
+constexpr int kMaxTileRows = 1024;
+
+// Fine-grid offsets of the rows of the padded tile at origin o (periodic
+// wrap), computed once per subproblem so that the per-transform tile loads
+// need no integer division.  Returns the table, or nullptr if the tile has
+// more rows than the table holds.  The caller synchronises before use.
+template <int DIM>
+__device__ __forceinline__ const int* tile_rows_init(const Geom& g, const int* o, int* table) {
+  const int nrows = DIM == 2 ? g.pd[0] : g.pd[0] * g.pd[1];
+  if (nrows > kMaxTileRows) return nullptr;
+  for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+    int off;
+    if (DIM == 2) {
+      off = wrap_idx(o[0] + r, g.nf[0]) * g.nf[1];
+    } else {
+      const int i1 = r % g.pd[1];
+      const int i0 = r / g.pd[1];
+      off = (wrap_idx(o[0] + i0, g.nf[0]) * g.nf[1] + wrap_idx(o[1] + i1, g.nf[1])) * g.nf[2];
+    }
+    table[r] = off;  // fine grids hold < 2^31 cells
+  }
+  return table;
+}
+
 // Stage the padded tiles of `nc` transforms (from transform c0 on) into shared
 // memory.  Rows of the tile (all axes but the last) are spread over groups of
-// `seg` threads, seg = a power of two >= the last tile extent, so that each
-// row costs one index decomposition and the row's cells load contiguously.
+// `seg` threads, seg = a power of two >= the last tile extent, so that the
+// row's cells load contiguously.  Row offsets come from `rowoff` (see
+// tile_rows_init) when given.
 template <int DIM>
 __device__ __forceinline__ void load_tiles(float2* tile, const float2* __restrict__ fine,
-                                           const Geom& g, const int* o, int c0, int nc) {
+                                           const Geom& g, const int* o, int c0, int nc,
+                                           const int* rowoff = nullptr) {
   const int last = DIM - 1;
   const int pl = g.pd[last];
   int seg = 16;
   while (seg < pl) seg <<= 1;
   const int rows_per_tile = DIM == 2 ? g.pd[0] : g.pd[0] * g.pd[1];
-  const int nrows = nc * rows_per_tile;
   const int col = threadIdx.x & (seg - 1);
   const int step = blockDim.x / seg;
-  const int mc = col < pl ? wrap_idx(o[last] + col, g.nf[last]) : 0;
+  if (col >= pl) return;
+  const int mc = wrap_idx(o[last] + col, g.nf[last]);
+  if (rowoff) {
+    for (int cc = 0; cc < nc; ++cc) {
+      const float2* src = fine + (int64_t)(c0 + cc) * g.G + mc;
+      float2* dst = tile + cc * rows_per_tile * pl + col;
+      for (int r = threadIdx.x / seg; r < rows_per_tile; r += step) dst[r * pl] = src[rowoff[r]];
+    }
+    return;
+  }
+  const int nrows = nc * rows_per_tile;
   for (int r = threadIdx.x / seg; r < nrows; r += step) {
-    if (col >= pl) continue;
     const int cc = r / rows_per_tile;
     const int rr = r - cc * rows_per_tile;
     int64_t rowbase;
@@ -122,6 +158,47 @@ __device__ __forceinline__ void load_tiles(float2* tile, const float2* __restric
                 g.nf[2];
     }
     tile[(int64_t)r * pl + col] = fine[(int64_t)(c0 + cc) * g.G + rowbase + mc];
+  }
+}
+
+// Asynchronous global -> shared copies of one tile (cp.async, 8 bytes per
+// cell), with the same row / column split as load_tiles.
+__device__ __forceinline__ void cp_async8(float2* dst, const float2* src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int DIM>
+__device__ __forceinline__ void load_tile_async(float2* tile, const float2* __restrict__ fine,
+                                                const Geom& g, const int* o, const int* rowoff) {
+  const int last = DIM - 1;
+  const int pl = g.pd[last];
+  int seg = 16;
+  while (seg < pl) seg <<= 1;
+  const int nrows = DIM == 2 ? g.pd[0] : g.pd[0] * g.pd[1];
+  const int col = threadIdx.x & (seg - 1);
+  if (col >= pl) return;
+  const int step = blockDim.x / seg;
+  const int mc = wrap_idx(o[last] + col, g.nf[last]);
+  if (rowoff) {
+    for (int r = threadIdx.x / seg; r < nrows; r += step)
+      cp_async8(tile + r * pl + col, fine + rowoff[r] + mc);
+    return;
+  }
+  for (int r = threadIdx.x / seg; r < nrows; r += step) {
+    int64_t rowbase;
+    if (DIM == 2) {
+      rowbase = (int64_t)wrap_idx(o[0] + r, g.nf[0]) * g.nf[1];
+    } else {
+      const int i1 = r % g.pd[1];
+      const int i0 = r / g.pd[1];
+      rowbase = ((int64_t)wrap_idx(o[0] + i0, g.nf[0]) * g.nf[1] + wrap_idx(o[1] + i1, g.nf[1])) *
+                g.nf[2];
+    }
+    cp_async8(tile + r * pl + col, fine + rowbase + mc);
   }
 }
 
@@ -142,9 +219,22 @@ __device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) 
   const int w = W > 0 ? W : g.w;
   const int WL = W > 0 ? W : w;
 
+  __shared__ int s_rowoff[kMaxTileRows];
+  const int* rowoff = tile_rows_init<DIM>(g, o, s_rowoff);
+  __syncthreads();
+
   for (int c0 = 0; c0 < a.ntr; c0 += CG) {
     const int nc = imin(CG, a.ntr - c0);
-    load_tiles<DIM>(tile, a.fine, g, o, c0, nc);
+    const float2* cur = tile;
+    if (rowoff) {
+      // asynchronous copies: every cell of the tile in flight at once
+      for (int cc = 0; cc < nc; ++cc)
+        load_tile_async<DIM>(tile + cc * T, a.fine + (int64_t)(c0 + cc) * g.G, g, o, rowoff);
+      cp_async_commit();
+      cp_async_wait<0>();
+    } else {
+      load_tiles<DIM>(tile, a.fine, g, o, c0, nc);
+    }
     __syncthreads();
     for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
       const int pos = p0 + s;
@@ -160,7 +250,7 @@ GBN_UNROLL
 GBN_UNROLL
         for (int t0 = 0; t0 < WL; ++t0) {
           {
-            const float2* row = tile + (l0 + t0) * g.pd[1] + l1;
+            const float2* row = cur + (l0 + t0) * g.pd[1] + l1;
 GBN_UNROLL
             for (int cc = 0; cc < CG; ++cc) {
               float sr = 0.f, si = 0.f;
@@ -185,7 +275,7 @@ GBN_UNROLL
             for (int t1 = 0; t1 < WL; ++t1) {
               {
                 const float wy = w0[t0] * w1[t1];
-                const float2* row = tile + ((l0 + t0) * g.pd[1] + (l1 + t1)) * g.pd[2] + l2;
+                const float2* row = cur + ((l0 + t0) * g.pd[1] + (l1 + t1)) * g.pd[2] + l2;
 GBN_UNROLL
                 for (int cc = 0; cc < CG; ++cc) {
                   float sr = 0.f, si = 0.f;
@@ -248,40 +338,6 @@ interp_kernel(InterpArgs a) {
 // transform c+1 streams into shared memory with cp.async while transform c
 // is interpolated.  maxsub <= S * GBN_THREADS.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async8(float2* dst, const float2* src) {
-  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-template <int DIM>
-__device__ __forceinline__ void load_tile_async(float2* tile, const float2* __restrict__ fine,
-                                                const Geom& g, const int* o) {
-  const int last = DIM - 1;
-  const int pl = g.pd[last];
-  int seg = 16;
-  while (seg < pl) seg <<= 1;
-  const int nrows = DIM == 2 ? g.pd[0] : g.pd[0] * g.pd[1];
-  const int col = threadIdx.x & (seg - 1);
-  if (col >= pl) return;
-  const int step = blockDim.x / seg;
-  const int mc = wrap_idx(o[last] + col, g.nf[last]);
-  for (int r = threadIdx.x / seg; r < nrows; r += step) {
-    int64_t rowbase;
-    if (DIM == 2) {
-      rowbase = (int64_t)wrap_idx(o[0] + r, g.nf[0]) * g.nf[1];
-    } else {
-      const int i1 = r % g.pd[1];
-      const int i0 = r / g.pd[1];
-      rowbase = ((int64_t)wrap_idx(o[0] + i0, g.nf[0]) * g.nf[1] + wrap_idx(o[1] + i1, g.nf[1])) *
-                g.nf[2];
-    }
-    cp_async8(tile + r * pl + col, fine + rowbase + mc);
-  }
-}
-
 template <int DIM, int W, int S>
 __global__ void __launch_bounds__(GBN_THREADS)
 interp_db_kernel(InterpArgs a) {
@@ -309,11 +365,14 @@ interp_db_kernel(InterpArgs a) {
       if (DIM == 3) l2[q] = weights_rt<W>(a.s.u[2][pos], g, w2[q]) - o[2];
     }
   }
-  load_tile_async<DIM>(tiles, a.fine, g, o);
+  __shared__ int s_rowoff[kMaxTileRows];
+  const int* rowoff = tile_rows_init<DIM>(g, o, s_rowoff);
+  __syncthreads();
+  load_tile_async<DIM>(tiles, a.fine, g, o, rowoff);
   cp_async_commit();
   for (int c = 0; c < a.ntr; ++c) {
     if (c + 1 < a.ntr) {
-      load_tile_async<DIM>(tiles + ((c + 1) & 1) * T, a.fine + (int64_t)(c + 1) * g.G, g, o);
+      load_tile_async<DIM>(tiles + ((c + 1) & 1) * T, a.fine + (int64_t)(c + 1) * g.G, g, o, rowoff);
       cp_async_commit();
       cp_async_wait<1>();
     } else {
@@ -626,9 +685,11 @@ interp_twc3d_kernel(InterpArgs a) {
   const int q = lane >> 3, l = lane & 7;
   const int ngroups = (cnt + 3) >> 2;
   const int pd12 = g.pd[1] * g.pd[2];
+  __shared__ int s_rowoff[kMaxTileRows];
+  const int* rowoff = tile_rows_init<3>(g, o, s_rowoff);
   for (int c = 0; c < a.ntr; ++c) {
-    __syncthreads();  // previous tile consumed, sample table written
-    load_tiles<3>(tile, a.fine, g, o, c, 1);
+    __syncthreads();  // previous tile consumed, sample and row tables written
+    load_tiles<3>(tile, a.fine, g, o, c, 1, rowoff);
     __syncthreads();
     for (int gi = warp; gi < ngroups; gi += (GBN_THREADS / 32)) {
       const int s = gi * 4 + q;
@@ -1152,8 +1213,11 @@ grad_kernel(GradArgs a, int conj_a) {
   const int w = W > 0 ? W : g.w;
   const int WL = W > 0 ? W : w;
 
+  __shared__ int s_rowoff[kMaxTileRows];
+  const int* rowoff = tile_rows_init<DIM>(g, o, s_rowoff);
+  __syncthreads();
   for (int c = 0; c < a.ntr; ++c) {
-    load_tiles<DIM>(tile, a.fine, g, o, c, 1);
+    load_tiles<DIM>(tile, a.fine, g, o, c, 1, rowoff);
     __syncthreads();
     for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
       const int pos = p0 + s;
