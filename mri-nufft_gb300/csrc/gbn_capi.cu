@@ -216,6 +216,16 @@ struct gbn_plan_s {
 
   std::map<int, cufftHandle> ffts;
 
+  // Pruned 3D transforms.  The image occupies the planes |n0| < N0/2 of
+  // axis 0 (indices [0, lo) and [nf0 - hi, nf0)), so a transform whose input
+  // is confined there (after padding) runs 2D (axes 1, 2) FFTs over those
+  // planes only, then 1D FFTs along axis 0; a transform whose output is only
+  // read there (before cropping) runs the same two steps in reverse order.
+  // The planes of consecutive transforms' hi and lo ranges are contiguous,
+  // so T transforms take T + 1 batched 2D calls.
+  bool prune = false;
+  cufftHandle pl_lo = 0, pl_span = 0, pl_hi = 0, pl_x = 0;
+
   // per-stage CUDA-event timing (gbn_profile) and kernel launch count
   bool prof = false;
   std::vector<cudaEvent_t> evpool;
@@ -236,6 +246,8 @@ struct gbn_plan_s {
   ~gbn_plan_s() {
     for (auto e : evpool) cudaEventDestroy(e);
     for (auto& kv : ffts) cufftDestroy(kv.second);
+    for (cufftHandle h : {pl_lo, pl_span, pl_hi, pl_x})
+      if (h) cufftDestroy(h);
     for (int d = 0; d < 3; ++d) dev_free(dec[d]);
     dev_free(fine);
     dev_free(kbuf);
@@ -330,7 +342,33 @@ struct gbn_plan_s {
     return h;
   }
 
-  void exec_fft(int batch, float2* data, int isign, cudaStream_t st);
+  // prune_mode: 0 full transform, 1 input confined to the image planes,
+  // 2 output read on the image planes only
+  void exec_fft(int batch, float2* data, int isign, cudaStream_t st, int prune_mode = 0);
+
+  cufftHandle make_plan(int rank, int* n, int* embed, int stride, int dist, int batch) {
+    cufftHandle h;
+    ckfft(cufftPlanMany(&h, rank, n, embed, stride, dist, embed, stride, dist, CUFFT_C2C, batch),
+          "cufftPlanMany");
+    size_t ws = 0;
+    cufftGetSize(h, &ws);
+    bytes += (int64_t)ws;
+    return h;
+  }
+
+  void make_pruned_plans() {
+    const int lo = g.n[0] - g.n[0] / 2, hi = g.n[0] / 2;
+    const int P = g.nf[1] * g.nf[2];
+    int n2[2] = {g.nf[1], g.nf[2]};
+    pl_lo = make_plan(2, n2, nullptr, 1, P, lo);
+    if (hi > 0) {
+      pl_span = make_plan(2, n2, nullptr, 1, P, lo + hi);
+      pl_hi = make_plan(2, n2, nullptr, 1, P, hi);
+    }
+    int n1[1] = {g.nf[0]};
+    int e1[1] = {g.nf[0]};
+    pl_x = make_plan(1, n1, e1, P, 1, P);
+  }
 };
 
 // Records CUDA events around one stage launch when profiling is enabled.
@@ -350,8 +388,40 @@ struct Span {
   }
 };
 
-void gbn_plan_s::exec_fft(int batch, float2* data, int isign, cudaStream_t st) {
+void gbn_plan_s::exec_fft(int batch, float2* data, int isign, cudaStream_t st, int prune_mode) {
     Span span(this, GBN_STAGE_FFT, st);
+    if (prune && prune_mode != 0) {
+      if (!pl_x) make_pruned_plans();
+      const int dir = isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE;
+      auto run = [&](cufftHandle h, float2* d) {
+        ckfft(cufftSetStream(h, st), "cufftSetStream");
+        ckfft(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(d), reinterpret_cast<cufftComplex*>(d),
+                           dir),
+              "cufftExecC2C");
+      };
+      const int64_t P = (int64_t)g.nf[1] * g.nf[2];
+      const int hi = g.n[0] / 2;
+      auto planes = [&]() {
+        if (hi == 0) {
+          for (int t = 0; t < batch; ++t) run(pl_lo, data + t * g.G);
+          return;
+        }
+        run(pl_lo, data);
+        for (int t = 0; t + 1 < batch; ++t) run(pl_span, data + t * g.G + (g.nf[0] - hi) * P);
+        run(pl_hi, data + (batch - 1) * g.G + (g.nf[0] - hi) * P);
+      };
+      auto columns = [&]() {
+        for (int t = 0; t < batch; ++t) run(pl_x, data + t * g.G);
+      };
+      if (prune_mode == 1) {
+        planes();
+        columns();
+      } else {
+        columns();
+        planes();
+      }
+      return;
+    }
     cufftHandle h = fft(batch);
     ckfft(cufftSetStream(h, st), "cufftSetStream");
     ckfft(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data),
@@ -604,6 +674,10 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
            "copy deconv factors");
       }
     }
+    {
+      const char* e = std::getenv("GBN_FFT_PRUNE");
+      p->prune = dim == 3 && !spread_only && g.nf[0] > g.n[0] && !(e && std::atoi(e) == 0);
+    }
     p->fine = dev_alloc<float2>((size_t)ntrans * g.G, p->bytes, "fine grid");
     p->setup_bins();
     p->sb.d_total = dev_alloc<int>(2, p->bytes, "scan");
@@ -755,7 +829,7 @@ int gbn_op(gbn_plan p, const void* img, const void* smaps, void* ksp, int B, int
       PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                      : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
       run_pad(p, pa, st);
-      p->exec_fft(T, p->fine, isign, st);
+      p->exec_fft(T, p->fine, isign, st, 1);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       run_interp(p, interp_args(p, p->fine, y + row * p->M, T, scale, INTERP_STORE), st);
     });
@@ -787,7 +861,7 @@ int gbn_adj(gbn_plan p, const void* ksp, const float* density, const void* smaps
       run_zero(p, p->fine, (size_t)T * g.G, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       run_spread(p, spread_args(p, y + row * p->M, density, p->fine, T, 1.0f), st);
-      p->exec_fft(T, p->fine, isign, st);
+      p->exec_fft(T, p->fine, isign, st, 2);
       CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, x + (int64_t)b * g.Nimg, T,
                                   c0 > 0, scale)
                       : crop_args(p, nullptr, x + (int64_t)c0 * g.Nimg, T, 0, scale);
@@ -822,7 +896,7 @@ int gbn_dc(gbn_plan p, const void* img, const void* obs, const float* density,
       PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                      : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
       run_pad(p, pa, st);
-      p->exec_fft(T, p->fine, -1, st);
+      p->exec_fft(T, p->fine, -1, st, 1);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       InterpArgs ia = interp_args(p, p->fine, p->kbuf, T, scale, INTERP_RESID);
       ia.obs = yo + row * p->M;
@@ -830,7 +904,7 @@ int gbn_dc(gbn_plan p, const void* img, const void* obs, const float* density,
       run_interp(p, ia, st);
       run_zero(p, p->fine, (size_t)T * g.G, st);
       run_spread(p, spread_args(p, p->kbuf, nullptr, p->fine, T, 1.0f), st);
-      p->exec_fft(T, p->fine, +1, st);
+      p->exec_fft(T, p->fine, +1, st, 2);
       CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, gr + (int64_t)b * g.Nimg, T,
                                   c0 > 0, scale)
                       : crop_args(p, nullptr, gr + (int64_t)c0 * g.Nimg, T, 0, scale);
@@ -866,7 +940,7 @@ static void grad_traj_common(gbn_plan p, const float2* img, const float2* s, con
     PadArgs pa = s ? pad_args(p, img + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, adjoint)
                    : pad_args(p, img + (int64_t)c0 * g.Nimg, nullptr, T, adjoint);
     run_pad(p, pa, st);
-    p->exec_fft(T, p->fine, adjoint ? +1 : -1, st);
+    p->exec_fft(T, p->fine, adjoint ? +1 : -1, st, 1);
     int64_t row = s ? (int64_t)b * C + c0 : c0;
     GradArgs ga{};
     ga.g = g;

@@ -129,6 +129,25 @@ def test_3d_dense_columns_coil_counts(gpu_pkg, eps, tol, C):
         assert rel_l2(x[c, vox], ref) < tol
 
 
+def test_pruned_fft_equals_full_fft(gpu_pkg, monkeypatch):
+    # 3D transforms skip the all-zero planes of the padded grid; the result
+    # must equal the full 3D FFT's (op, adj_op, data_consistency; several
+    # transforms per pass so that the plane spans of neighbouring coils join)
+    rng = np.random.default_rng(17)
+    shape = (20, 17, 22)
+    M, B, C = 4000, 2, 3
+    s = rng.uniform(-0.5, 0.5, (M, 3)).astype(np.float32)
+    smaps = (rng.standard_normal((C, *shape)) + 1j * rng.standard_normal((C, *shape))).astype(np.complex64)
+    x = (rng.standard_normal((B, *shape)) + 1j * rng.standard_normal((B, *shape))).astype(np.complex64)
+    y = (rng.standard_normal((B, C, M)) + 1j * rng.standard_normal((B, C, M))).astype(np.complex64)
+    pruned = gpu_pkg.MRIGB300(s, shape, n_coils=C, n_batchs=B, smaps=smaps)
+    monkeypatch.setenv("GBN_FFT_PRUNE", "0")
+    full = gpu_pkg.MRIGB300(s, shape, n_coils=C, n_batchs=B, smaps=smaps)
+    assert rel_l2(pruned.op(x), full.op(x)) < 1e-5
+    assert rel_l2(pruned.adj_op(y), full.adj_op(y)) < 1e-5
+    assert rel_l2(pruned.data_consistency(x, y), full.data_consistency(x, y)) < 1e-5
+
+
 def test_density_and_boundaries(gpu_pkg):
     rng = np.random.default_rng(7)
     shape = (32, 32)
