@@ -205,6 +205,90 @@ __device__ __forceinline__ void load_tile_async(float2* tile, const float2* __re
 // ---------------------------------------------------------------------------
 // Interpolation
 // ---------------------------------------------------------------------------
+// Footprint sum of one sample over the staged tiles of CG transforms.
+template <int DIM, int W, int CG>
+__device__ __forceinline__ void interp_footprint(const float2* cur, const Geom& g, int T,
+                                                 const float* w0, const float* w1, const float* w2,
+                                                 int l0, int l1, int l2, float* ar, float* ai) {
+  const int WL = W > 0 ? W : g.w;
+GBN_UNROLL
+  for (int cc = 0; cc < CG; ++cc) { ar[cc] = 0.f; ai[cc] = 0.f; }
+  if (DIM == 2) {
+GBN_UNROLL
+    for (int t0 = 0; t0 < WL; ++t0) {
+      const float2* row = cur + (l0 + t0) * g.pd[1] + l1;
+GBN_UNROLL
+      for (int cc = 0; cc < CG; ++cc) {
+        float sr = 0.f, si = 0.f;
+GBN_UNROLL
+        for (int t1 = 0; t1 < WL; ++t1) {
+          float2 v = row[cc * T + t1];
+          sr = fmaf(w1[t1], v.x, sr);
+          si = fmaf(w1[t1], v.y, si);
+        }
+        ar[cc] = fmaf(w0[t0], sr, ar[cc]);
+        ai[cc] = fmaf(w0[t0], si, ai[cc]);
+      }
+    }
+  } else {
+GBN_UNROLL
+    for (int t0 = 0; t0 < WL; ++t0) {
+GBN_UNROLL
+      for (int t1 = 0; t1 < WL; ++t1) {
+        const float wy = w0[t0] * w1[t1];
+        const float2* row = cur + ((l0 + t0) * g.pd[1] + (l1 + t1)) * g.pd[2] + l2;
+GBN_UNROLL
+        for (int cc = 0; cc < CG; ++cc) {
+          float sr = 0.f, si = 0.f;
+GBN_UNROLL
+          for (int t2 = 0; t2 < WL; ++t2) {
+            float2 v = row[cc * T + t2];
+            sr = fmaf(w2[t2], v.x, sr);
+            si = fmaf(w2[t2], v.y, si);
+          }
+          ar[cc] = fmaf(wy, sr, ar[cc]);
+          ai[cc] = fmaf(wy, si, ai[cc]);
+        }
+      }
+    }
+  }
+}
+
+// Interp epilogue of one sample (original index j) for transforms c0 .. c0+nc-1.
+template <int CG>
+__device__ __forceinline__ void interp_store(const InterpArgs& a, int j, int c0, int nc,
+                                             const float* ar, const float* ai) {
+  if (a.mode == INTERP_PIPE) {
+    // single transform: w_j <- w_j / |scale * v_j|
+    float2 cur = a.out[j];
+    float mag = a.scale * sqrtf(ar[0] * ar[0] + ai[0] * ai[0]);
+    a.out[j] = make_float2(cur.x / mag, cur.y / mag);
+    return;
+  }
+GBN_UNROLL
+  for (int cc = 0; cc < CG; ++cc) {
+    if (cc < nc) {
+      const int64_t oi = (int64_t)(c0 + cc) * a.s.M + j;
+      float2 r = make_float2(a.scale * ar[cc], a.scale * ai[cc]);
+      if (a.mode == INTERP_RESID) {
+        float2 ob = a.obs[oi];
+        r.x -= ob.x;
+        r.y -= ob.y;
+        if (a.density) {
+          float dj = a.density[j];
+          r.x *= dj;
+          r.y *= dj;
+        }
+      }
+      a.out[oi] = r;
+    }
+  }
+}
+
+// One CTA per subproblem.  When the subproblem has at most one sample per
+// thread, each thread evaluates its sample's kernel weights once and keeps
+// them in registers for every transform pass; larger subproblems evaluate
+// them per pass.
 template <int DIM, int W, int CG>
 __device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) {
   constexpr int WM = WidthTraits<W>::WM;
@@ -216,16 +300,24 @@ __device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) 
   int o[3];
   bin_origin<DIM>(g, b, o);
   const int T = g.tile;
-  const int w = W > 0 ? W : g.w;
-  const int WL = W > 0 ? W : w;
 
   __shared__ int s_rowoff[kMaxTileRows];
   const int* rowoff = tile_rows_init<DIM>(g, o, s_rowoff);
+
+  const bool cached = cnt <= (int)blockDim.x;
+  float cw0[WM], cw1[WM], cw2[WM];
+  int cl0 = 0, cl1 = 0, cl2 = 0, cj = -1;
+  if (cached && (int)threadIdx.x < cnt) {
+    const int pos = p0 + threadIdx.x;
+    cl0 = weights_rt<W>(a.s.u[0][pos], g, cw0) - o[0];
+    cl1 = weights_rt<W>(a.s.u[1][pos], g, cw1) - o[1];
+    if (DIM == 3) cl2 = weights_rt<W>(a.s.u[2][pos], g, cw2) - o[2];
+    cj = a.s.perm[pos];
+  }
   __syncthreads();
 
   for (int c0 = 0; c0 < a.ntr; c0 += CG) {
     const int nc = imin(CG, a.ntr - c0);
-    const float2* cur = tile;
     if (rowoff) {
       // asynchronous copies: every cell of the tile in flight at once
       for (int cc = 0; cc < nc; ++cc)
@@ -236,98 +328,33 @@ __device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) 
       load_tiles<DIM>(tile, a.fine, g, o, c0, nc);
     }
     __syncthreads();
-    for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
-      const int pos = p0 + s;
-      float w0[WM], w1[WM], w2[WM];
-      int l0 = weights_rt<W>(a.s.u[0][pos], g, w0) - o[0];
-      int l1 = weights_rt<W>(a.s.u[1][pos], g, w1) - o[1];
-      int l2 = 0;
-      if (DIM == 3) l2 = weights_rt<W>(a.s.u[2][pos], g, w2) - o[2];
-      float ar[CG], ai[CG];
-GBN_UNROLL
-      for (int cc = 0; cc < CG; ++cc) { ar[cc] = 0.f; ai[cc] = 0.f; }
-      if (DIM == 2) {
-GBN_UNROLL
-        for (int t0 = 0; t0 < WL; ++t0) {
-          {
-            const float2* row = cur + (l0 + t0) * g.pd[1] + l1;
-GBN_UNROLL
-            for (int cc = 0; cc < CG; ++cc) {
-              float sr = 0.f, si = 0.f;
-GBN_UNROLL
-              for (int t1 = 0; t1 < WL; ++t1) {
-                {
-                  float2 v = row[cc * T + t1];
-                  sr = fmaf(w1[t1], v.x, sr);
-                  si = fmaf(w1[t1], v.y, si);
-                }
-              }
-              ar[cc] = fmaf(w0[t0], sr, ar[cc]);
-              ai[cc] = fmaf(w0[t0], si, ai[cc]);
-            }
-          }
-        }
-      } else {
-GBN_UNROLL
-        for (int t0 = 0; t0 < WL; ++t0) {
-          {
-GBN_UNROLL
-            for (int t1 = 0; t1 < WL; ++t1) {
-              {
-                const float wy = w0[t0] * w1[t1];
-                const float2* row = cur + ((l0 + t0) * g.pd[1] + (l1 + t1)) * g.pd[2] + l2;
-GBN_UNROLL
-                for (int cc = 0; cc < CG; ++cc) {
-                  float sr = 0.f, si = 0.f;
-GBN_UNROLL
-                  for (int t2 = 0; t2 < WL; ++t2) {
-                    {
-                      float2 v = row[cc * T + t2];
-                      sr = fmaf(w2[t2], v.x, sr);
-                      si = fmaf(w2[t2], v.y, si);
-                    }
-                  }
-                  ar[cc] = fmaf(wy, sr, ar[cc]);
-                  ai[cc] = fmaf(wy, si, ai[cc]);
-                }
-              }
-            }
-          }
-        }
+    float ar[CG], ai[CG];
+    if (cached) {
+      if (cj >= 0) {
+        interp_footprint<DIM, W, CG>(tile, g, T, cw0, cw1, cw2, cl0, cl1, cl2, ar, ai);
+        interp_store<CG>(a, cj, c0, nc, ar, ai);
       }
-      const int j = a.s.perm[pos];
-      if (a.mode == INTERP_PIPE) {
-        // single transform: w_j <- w_j / |scale * v_j|
-        float2 cur = a.out[j];
-        float mag = a.scale * sqrtf(ar[0] * ar[0] + ai[0] * ai[0]);
-        a.out[j] = make_float2(cur.x / mag, cur.y / mag);
-      } else {
-GBN_UNROLL
-        for (int cc = 0; cc < CG; ++cc) {
-          if (cc < nc) {
-            const int64_t oi = (int64_t)(c0 + cc) * a.s.M + j;
-            float2 r = make_float2(a.scale * ar[cc], a.scale * ai[cc]);
-            if (a.mode == INTERP_RESID) {
-              float2 ob = a.obs[oi];
-              r.x -= ob.x;
-              r.y -= ob.y;
-              if (a.density) {
-                float dj = a.density[j];
-                r.x *= dj;
-                r.y *= dj;
-              }
-            }
-            a.out[oi] = r;
-          }
-        }
+    } else {
+      for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
+        const int pos = p0 + s;
+        float w0[WM], w1[WM], w2[WM];
+        int l0 = weights_rt<W>(a.s.u[0][pos], g, w0) - o[0];
+        int l1 = weights_rt<W>(a.s.u[1][pos], g, w1) - o[1];
+        int l2 = 0;
+        if (DIM == 3) l2 = weights_rt<W>(a.s.u[2][pos], g, w2) - o[2];
+        interp_footprint<DIM, W, CG>(tile, g, T, w0, w1, w2, l0, l1, l2, ar, ai);
+        interp_store<CG>(a, a.s.perm[pos], c0, nc, ar, ai);
       }
     }
     __syncthreads();
   }
 }
 
+// 128-thread CTAs; at least 5 resident per SM keeps registers <= 96 a thread
+constexpr int kInterpThreads = 128;
+
 template <int DIM, int W, int CG>
-__global__ void __launch_bounds__(GBN_THREADS)
+__global__ void __launch_bounds__(kInterpThreads, 5)
 interp_kernel(InterpArgs a) {
   interp_body<DIM, W, CG>(a, blockIdx.x);
 }
@@ -1288,7 +1315,7 @@ cudaError_t launch_interp_t(const InterpArgs& a, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   // 128-thread CTAs: subproblems average fewer samples than 256, and smaller
   // CTAs wait less at the per-coil tile barriers (measured 4 % faster in 3D)
-  const int threads = a.g.interp_threads > 0 ? a.g.interp_threads : 128;
+  const int threads = a.g.interp_threads == 64 ? 64 : kInterpThreads;
   k<<<a.s.nsub, threads, smem, st>>>(a);
   return cudaGetLastError();
 }
