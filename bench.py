@@ -56,9 +56,10 @@ def parse():
     p.add_argument("--rate", type=float, default=50.0, help="c5: Poisson arrival rate (req/s)")
     p.add_argument("--saturated", type=int, default=300,
                    help="c5: requests of the saturated served-vs-plain comparison")
-    p.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
-                   help="c2: 3D 16-coil SENSE (default line); c3: 32 uneven 2D instances, "
-                        "batched graph-captured launch vs per-call loop")
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                   help="c2: 3D 16-coil SENSE (default line); c1: 2D 256^2 single-coil radial; "
+                        "c3: 32 uneven 2D instances, batched graph-captured launch vs per-call "
+                        "loop; c4: differentiable forward+backward; c5: served CG stream")
     return p.parse_args()
 
 
@@ -405,6 +406,119 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed_steps(fn, steps, warmup, flush):
+    """Per-step CUDA-event times of fn() with an L2 flush (a write larger
+    than L2) between steps, outside the timed spans; returns ms per step."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    for a, b in evs:
+        flush.zero_()
+        a.record()
+        fn()
+        b.record()
+    torch.cuda.synchronize()
+    return float(np.mean([a.elapsed_time(b) for a, b in evs]))
+
+
+def run_c1(args):
+    """2D 256^2 single coil, radial 100 x 500 (50 000 samples): op + adj."""
+    import torch
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    __graft_entry__.build()
+    pkg = __graft_entry__.import_package()
+    from mrinufft_gb300 import workloads
+
+    traj, shape, img = workloads.config1()
+    M = traj.shape[0]
+    op = pkg.MRIGB300(traj, shape, squeeze_dims=False)
+    x = torch.from_numpy(img).to(dev).reshape(1, 1, *shape)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    steps = max(args.steps, 100)
+    ms = _timed_steps(lambda: op._adj_device(op._op_device(x)), steps, max(args.warmup, 3), flush)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import esnufft
+
+        ncores = os.cpu_count() or 1
+        e = esnufft.EsNufft(traj.astype(np.float64) * 2 * np.pi, shape, dtype=np.float32,
+                            nthreads=ncores)
+        nrm = np.sqrt(np.prod(shape) * 4)
+        t = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            _ = e.type1(e.type2(img) / nrm) / nrm
+        dt = (time.perf_counter() - t) / reps
+        cpu = {"value": M / dt / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
+               "sample": f"{reps} op+adj steps, C/OpenMP ES spreader + scipy.fft"}
+    line = {
+        "metric": METRIC, "value": M / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1,
+        "steps": steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (radial 100 x 500, ellipse phantom)",
+        "config": {"workload": "2D 256^2 single coil, radial 100x500 (50 000 samples), op+adj",
+                   "l2": "flushed between steps (256 MB write)"},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_c4(args):
+    """Differentiable form: 256^2, 8 coils, spiral 64 x 2048 (131 072 samples);
+    loss ||A(x) - y||^2 with gradients for the image and the trajectory."""
+    import torch
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    __graft_entry__.build()
+    pkg = __graft_entry__.import_package()
+    from mrinufft_gb300 import workloads
+
+    shape, C = (256, 256), 8
+    traj = workloads.spiral_2d(64, 2048, power=2).reshape(-1, 2).astype(np.float32)
+    M = traj.shape[0]
+    smaps = workloads.coil_maps(shape, C, seed=4)
+    img = workloads.phantom(shape, seed=4)
+    nufft = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps, squeeze_dims=False)
+    rng = np.random.default_rng(4)
+    pert = traj + 1e-3 * rng.standard_normal(traj.shape).astype(np.float32)
+    y = pkg.MRIGB300(pert, shape, n_coils=C, smaps=smaps, squeeze_dims=False).op(img)
+    yt = torch.from_numpy(np.asarray(y)).to(dev).reshape(1, C, M)
+    ad = nufft.make_autograd(wrt_data=True, wrt_traj=True)
+    x0 = torch.from_numpy(img).to(dev).reshape(1, 1, *shape)
+
+    def step():
+        x = x0.clone().requires_grad_(True)
+        if ad.samples.grad is not None:
+            ad.samples.grad = None
+        loss = torch.sum(torch.abs(ad.op(x) - yt) ** 2)
+        loss.backward()
+        return x.grad, ad.samples.grad
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ms = _timed_steps(step, max(args.steps, 50), max(args.warmup, 3), flush)
+    line = {
+        "metric": "differentiable NUFFT forward+backward Msamples*coil/s (grads wrt image and trajectory)",
+        "value": M * C / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1, "steps": max(args.steps, 50),
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (Galilean spiral 64 x 2048, ellipse phantom, Gaussian coil maps, "
+                "k-space from a 1e-3-perturbed trajectory)",
+        "config": {"workload": "2D 256^2, 8 coils, spiral 64x2048 (131 072 samples); "
+                               "loss |A(x) - y|^2, backward for x and the trajectory",
+                   "nufft_calls_per_step": "1 forward + 1 adjoint (image grad) + 2 gradient "
+                                           "interpolations (trajectory grad)",
+                   "l2": "flushed between steps (256 MB write)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def c5_templates(dev):
     """Request templates of the served mix: 2D 256^2 radial 256x512 with 8, 16,
     24 or 32 coils (70 %), 2D 384^2 spiral 32x4096 with 16 coils (20 %), 3D
@@ -514,8 +628,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c1":
+        run_c1(args)
     elif args.workload == "c3":
         run_c3(args)
+    elif args.workload == "c4":
+        run_c4(args)
     elif args.workload == "c5":
         run_c5(args)
     else:
