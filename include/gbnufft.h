@@ -185,6 +185,38 @@ int gbn_batch_adj(gbn_batch batch, gbn_stream stream);
 int gbn_batch_destroy(gbn_batch batch);
 
 /*
+ * Toeplitz embedding of the Gram operator A^H W A (toeplitz.py:35-96
+ * compute_toeplitz_kernel, 193-269 apply_toeplitz_kernel; base.py:315-363
+ * gram_op with toeplitz=True).  A^H W A x is the linear convolution of x
+ * with psf(m) = sum_j w_j exp(+i k_j . m), |m_d| < N_d, i.e. a circular
+ * convolution on a grid of nf_d >= 2 N_d - 1 cells per axis.
+ *
+ *   gbn_toep_create: psf = type-1 transform of the weights (null: ones) on
+ *     2N modes (a temporary plan sharing the trajectory k0..k2 of `plan`),
+ *     placed at lag m -> m mod nf on the circulant grid (nf = the smallest
+ *     even 2-3-5-smooth size >= 2N), then kernel K = Re(FFT(psf)) (real for
+ *     real weights).  The handle owns K and fine grids for plan's ntrans.
+ *   gbn_toep_apply: per coil pass, zero-pad (x * s_c) into the circulant
+ *     grid, FFT, multiply by K, inverse FFT, crop with conj(s_c) coil sum
+ *     (smaps null: calibrationless, one image per coil), times
+ *     scale / prod(nf).  A^H W A x = apply(x) with scale 1 (times the
+ *     operator's 1/norm^2).
+ *   gbn_toep_info: nf per axis (unused axes 1);  gbn_toep_kernel: copies K
+ *     (prod(nf) floats, C order) into `dst` (device).
+ * The reference builds the same kernel from 2^(d-1) modulated adjoints on
+ * the N grid and keeps its real spectrum on the 2N grid; where nf = 2N the
+ * two kernels hold the same values.
+ */
+typedef struct gbn_toep_s* gbn_toep;
+int gbn_toep_create(gbn_plan plan, int64_t M, const float* k0, const float* k1, const float* k2,
+                    const float* weights, gbn_toep* out, gbn_stream stream);
+int gbn_toep_info(gbn_toep toep, int64_t* nf);
+int gbn_toep_kernel(gbn_toep toep, float* dst, gbn_stream stream);
+int gbn_toep_apply(gbn_toep toep, const void* img, const void* smaps, void* out, int B, int C,
+                   float scale, gbn_stream stream);
+int gbn_toep_destroy(gbn_toep toep);
+
+/*
  * Stage timing.  gbn_profile(plan, 1) clears the counters and records a pair
  * of CUDA events on the launch stream around every launch of a stage;
  * gbn_profile(plan, 0) stops recording.  gbn_profile_read waits for the
@@ -201,7 +233,8 @@ int gbn_batch_destroy(gbn_batch batch);
 #define GBN_STAGE_CROP 4
 #define GBN_STAGE_ZERO 5
 #define GBN_STAGE_GRAD 6
-#define GBN_STAGES 7
+#define GBN_STAGE_KMUL 7
+#define GBN_STAGES 8
 int gbn_profile(gbn_plan plan, int enable);
 int gbn_profile_read(gbn_plan plan, int stage, double* total_ms, int64_t* count);
 

@@ -25,7 +25,8 @@ GBN_ERR_CUFFT = 3
 GBN_ERR_NOMEM = 4
 GBN_ERR_STATE = 5
 
-STAGES = {"pad": 0, "fft": 1, "interp": 2, "spread": 3, "crop": 4, "zero": 5, "grad": 6}
+STAGES = {"pad": 0, "fft": 1, "interp": 2, "spread": 3, "crop": 4, "zero": 5, "grad": 6,
+          "kmul": 7}
 
 # name -> (restype, argtypes); must match include/gbnufft.h
 SIGNATURES = {
@@ -58,6 +59,11 @@ SIGNATURES = {
     "gbn_batch_op": (_c_int, [_vp, _vp]),
     "gbn_batch_adj": (_c_int, [_vp, _vp]),
     "gbn_batch_destroy": (_c_int, [_vp]),
+    "gbn_toep_create": (_c_int, [_vp, _c_i64, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp), _vp]),
+    "gbn_toep_info": (_c_int, [_vp, ctypes.POINTER(_c_i64)]),
+    "gbn_toep_kernel": (_c_int, [_vp, _vp, _vp]),
+    "gbn_toep_apply": (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _vp]),
+    "gbn_toep_destroy": (_c_int, [_vp]),
     "gbn_profile": (_c_int, [_vp, _c_int]),
     "gbn_profile_read": (_c_int, [_vp, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_i64)]),
     "gbn_norm2_f64": (_c_int, [_vp, _c_i64, _vp, _vp]),

@@ -1113,6 +1113,150 @@ int gbn_dotu_f64(const void* a, const void* b, int64_t n, int conj_a, double* ou
 }  // extern "C"
 
 // ----------------------------------------------------------------------------
+// Toeplitz embedding of A^H W A
+// ----------------------------------------------------------------------------
+struct gbn_toep_s {
+  gbn_plan inner = nullptr;  // circulant grid (n = N, nf >= 2N), FFT plans, fine grids
+  float* K = nullptr;        // real kernel spectrum, inner->g.G cells
+  int device = 0;
+  ~gbn_toep_s() {
+    DeviceGuard dg(device);
+    dev_free(K);
+    if (inner) gbn_plan_destroy(inner);
+  }
+};
+
+namespace {
+void chk(int rc) {
+  if (rc != GBN_OK) throw Fail{rc};  // the message is already set
+}
+}  // namespace
+
+extern "C" {
+
+int gbn_toep_create(gbn_plan p, int64_t M, const float* k0, const float* k1, const float* k2,
+                    const float* weights, gbn_toep* out, gbn_stream stream) {
+  if (!out) {
+    g_err = "null output handle";
+    return GBN_ERR_ARG;
+  }
+  *out = nullptr;
+  gbn_plan q = nullptr;
+  float2* w2 = nullptr;
+  float2* psf = nullptr;
+  gbn_toep t = nullptr;
+  int rc = guarded(p, [&] {
+    if (p->spread_only) fail(GBN_ERR_ARG, "the Toeplitz embedding needs a full NUFFT plan");
+    if (M < 0 || M > ((int64_t)1 << 31) - 1) fail(GBN_ERR_ARG, "M out of range");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const Geom& g = p->g;
+    int64_t n1[3] = {1, 1, 1}, n2[3] = {1, 1, 1};
+    int64_t P2 = 1;
+    for (int d = 0; d < g.dim; ++d) {
+      n1[d] = g.n[d];
+      n2[d] = 2 * (int64_t)g.n[d];
+      P2 *= n2[d];
+    }
+    int64_t tmp = 0;
+    // psf: type-1 transform of the weights on 2N modes
+    chk(gbn_plan_create(g.dim, n2, 2.0, p->eps, 1, 0, p->device, &q));
+    chk(gbn_setpts(q, M, k0, k1, k2, stream));
+    w2 = dev_alloc<float2>((size_t)M, tmp, "Toeplitz weights");
+    ck(launch_fill_weights(weights, w2, M, st), "Toeplitz weights");
+    psf = dev_alloc<float2>((size_t)P2, tmp, "Toeplitz psf");
+    chk(gbn_adj(q, w2, nullptr, nullptr, psf, 1, 1, 1.0f, +1, stream));
+    // circulant grid and the kernel spectrum
+    t = new gbn_toep_s();
+    t->device = p->device;
+    chk(gbn_plan_create(g.dim, n1, 2.0, p->eps, p->ntrans, 0, p->device, &t->inner));
+    gbn_plan in = t->inner;
+    ck(launch_toep_place(in->g, psf, in->fine, st), "Toeplitz placement");
+    in->exec_fft(1, in->fine, -1, st, 0);
+    int64_t kb = 0;
+    t->K = dev_alloc<float>((size_t)in->g.G, kb, "Toeplitz kernel");
+    in->bytes += kb;
+    ck(launch_real_part(in->fine, t->K, in->g.G, 1.0f, st), "Toeplitz kernel");
+    ck(cudaStreamSynchronize(st), "Toeplitz kernel sync");
+  });
+  {
+    DeviceGuard dg(p ? p->device : 0);
+    dev_free(w2);
+    dev_free(psf);
+    if (q) gbn_plan_destroy(q);
+  }
+  if (rc != GBN_OK) {
+    delete t;
+    return rc;
+  }
+  *out = t;
+  return GBN_OK;
+}
+
+int gbn_toep_info(gbn_toep t, int64_t* nf) {
+  if (!t || !nf) {
+    g_err = "null argument";
+    return GBN_ERR_ARG;
+  }
+  for (int d = 0; d < 3; ++d) nf[d] = t->inner->g.nf[d];
+  return GBN_OK;
+}
+
+int gbn_toep_kernel(gbn_toep t, float* dst, gbn_stream stream) {
+  if (!t || !dst) {
+    g_err = "null argument";
+    return GBN_ERR_ARG;
+  }
+  return guarded(t->inner, [&] {
+    ck(cudaMemcpyAsync(dst, t->K, sizeof(float) * t->inner->g.G, cudaMemcpyDeviceToDevice,
+                       reinterpret_cast<cudaStream_t>(stream)),
+       "copy Toeplitz kernel");
+  });
+}
+
+int gbn_toep_apply(gbn_toep t, const void* img, const void* smaps, void* out, int B, int C,
+                   float scale, gbn_stream stream) {
+  if (!t) {
+    g_err = "null Toeplitz handle";
+    return GBN_ERR_ARG;
+  }
+  gbn_plan p = t->inner;
+  return guarded(p, [&] {
+    check_counts(B, C);
+    if (!img || !out) fail(GBN_ERR_ARG, "null image pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const float2* x = static_cast<const float2*>(img);
+    const float2* s = static_cast<const float2*>(smaps);
+    float2* o = static_cast<float2*>(out);
+    const Geom& g = p->g;
+    const float sc = (float)((double)scale / (double)g.G);  // inverse-FFT normalisation
+    for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
+      PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
+                     : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
+      pa.dec[0] = pa.dec[1] = pa.dec[2] = nullptr;
+      run_pad(p, pa, st);
+      p->exec_fft(T, p->fine, -1, st, 1);
+      {
+        Span span(p, GBN_STAGE_KMUL, st);
+        ck(launch_kmul(p->fine, t->K, g.G, T, st), "Toeplitz multiply");
+        p->launches++;
+      }
+      p->exec_fft(T, p->fine, +1, st, 2);
+      CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, o + (int64_t)b * g.Nimg, T, c0 > 0, sc)
+                      : crop_args(p, nullptr, o + (int64_t)c0 * g.Nimg, T, 0, sc);
+      ca.dec[0] = ca.dec[1] = ca.dec[2] = nullptr;
+      run_crop(p, ca, st);
+    });
+  });
+}
+
+int gbn_toep_destroy(gbn_toep t) {
+  delete t;
+  return GBN_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------------------
 // Batches of independent plans
 // ----------------------------------------------------------------------------
 // Instances with the same fine grid share one contiguous pool of fine grids,

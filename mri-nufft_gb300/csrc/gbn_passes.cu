@@ -40,6 +40,86 @@ cudaError_t launch_crop(const CropArgs& a, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
+// Toeplitz embedding of A^H W A
+// ---------------------------------------------------------------------------
+// fine[t][i] *= K[i]: K is read once per cell for all ntr grids
+__global__ void kmul_kernel(float2* __restrict__ fine, const float* __restrict__ K, int64_t G,
+                            int ntr) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < G;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float k = K[i];
+    for (int t = 0; t < ntr; ++t) {
+      float2 v = fine[(int64_t)t * G + i];
+      fine[(int64_t)t * G + i] = make_float2(v.x * k, v.y * k);
+    }
+  }
+}
+
+// dst (circulant grid, nf per axis) <- psf (2N modes per axis, mode m at
+// array index m + N) for lags |m| < N at index m mod nf; other cells 0
+__global__ void toep_place_kernel(Geom gt, const float2* __restrict__ psf,
+                                  float2* __restrict__ dst) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= gt.G) return;
+  int64_t r = idx, src = 0;
+  bool inside = true;
+  int p[3] = {0, 0, 0};
+  for (int d = gt.dim - 1; d >= 0; --d) {
+    p[d] = (int)(r % gt.nf[d]);
+    r /= gt.nf[d];
+  }
+  for (int d = 0; d < gt.dim; ++d) {
+    const int N = gt.n[d], P = gt.nf[d];
+    int m;
+    if (p[d] < N) m = p[d];
+    else if (p[d] > P - N) m = p[d] - P;
+    else { inside = false; break; }
+    src = src * (2 * N) + (m + N);
+  }
+  dst[idx] = inside ? psf[src] : make_float2(0.f, 0.f);
+}
+
+__global__ void real_part_kernel(const float2* __restrict__ src, float* __restrict__ dst, int64_t n,
+                                 float scale) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i].x * scale;
+}
+
+__global__ void fill_weights_kernel(const float* __restrict__ w, float2* __restrict__ out,
+                                    int64_t M) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < M;
+       j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = make_float2(w ? w[j] : 1.0f, 0.0f);
+}
+
+static unsigned grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (unsigned)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+
+cudaError_t launch_kmul(float2* fine, const float* K, int64_t G, int ntr, cudaStream_t st) {
+  kmul_kernel<<<grid_for(G), 256, 0, st>>>(fine, K, G, ntr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_toep_place(const Geom& gt, const float2* psf, float2* dst, cudaStream_t st) {
+  toep_place_kernel<<<(unsigned)((gt.G + 255) / 256), 256, 0, st>>>(gt, psf, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_real_part(const float2* src, float* dst, int64_t n, float scale, cudaStream_t st) {
+  real_part_kernel<<<grid_for(n), 256, 0, st>>>(src, dst, n, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_weights(const float* w, float2* out, int64_t M, cudaStream_t st) {
+  if (M == 0) return cudaSuccess;
+  fill_weights_kernel<<<grid_for(M), 256, 0, st>>>(w, out, M);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // FP64 reductions (CG dot products and residual norms)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {

@@ -9,7 +9,7 @@ struct PadArgs {
   Geom g;
   const float2* img;    // SENSE: one image; calibrationless: ntr images
   const float2* smaps;  // SENSE: ntr coil maps (null: calibrationless)
-  const float* dec[3];  // 1/phihat per axis, indexed by image array index
+  const float* dec[3];  // 1/phihat per axis, indexed by image array index (null: 1)
   float2* fine;         // ntr fine grids (every cell written)
   int ntr;
   int conj_in;          // use conj(img) and conj(smaps)
@@ -20,7 +20,7 @@ struct CropArgs {
   Geom g;
   const float2* fine;   // ntr fine grids
   const float2* smaps;  // SENSE coil maps (null: calibrationless)
-  const float* dec[3];
+  const float* dec[3];  // 1/phihat per axis (null: 1)
   float2* out;          // SENSE: one image; calibrationless: ntr images
   int ntr;
   int accumulate;       // SENSE: out += result
@@ -60,7 +60,7 @@ __device__ __forceinline__ void pad_body(const PadArgs& a, const int64_t idx) {
     else { inside = false; break; }
     int i = n + h;
     ii = ii * g.n[d] + i;
-    f *= a.dec[d][i];
+    if (a.dec[d]) f *= a.dec[d][i];
   }
   if (!inside) {
     for (int c = 0; c < a.ntr; ++c) a.fine[(int64_t)c * g.G + idx] = make_float2(0.f, 0.f);
@@ -101,7 +101,7 @@ __device__ __forceinline__ void crop_body(const CropArgs& a, const int64_t idx) 
     int n = i[d] - g.n[d] / 2;
     int m = n < 0 ? n + g.nf[d] : n;
     mlin = mlin * g.nf[d] + m;
-    f *= a.dec[d][i[d]];
+    if (a.dec[d]) f *= a.dec[d][i[d]];
   }
   if (a.smaps) {
     float2 acc = make_float2(0.f, 0.f);
@@ -128,6 +128,14 @@ __device__ __forceinline__ void crop_body(const CropArgs& a, const int64_t idx) 
   }
 }
 
+// Toeplitz embedding helpers: fine[t][i] *= K[i] for ntr grids of G cells;
+// the lag-ordered placement of a type-1 transform on 2N modes into the
+// circulant grid gt (lags |m| < N at m mod nf, zero elsewhere); real part
+// with a scale; complex weights from real ones (null: ones).
+cudaError_t launch_kmul(float2* fine, const float* K, int64_t G, int ntr, cudaStream_t st);
+cudaError_t launch_toep_place(const Geom& gt, const float2* psf, float2* dst, cudaStream_t st);
+cudaError_t launch_real_part(const float2* src, float* dst, int64_t n, float scale, cudaStream_t st);
+cudaError_t launch_fill_weights(const float* w, float2* out, int64_t M, cudaStream_t st);
 cudaError_t launch_pad(const PadArgs& a, cudaStream_t st);
 cudaError_t launch_crop(const CropArgs& a, cudaStream_t st);
 cudaError_t launch_norm2(const float2* x, int64_t n, double* out, cudaStream_t st);

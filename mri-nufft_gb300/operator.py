@@ -106,6 +106,8 @@ class MRIGB300(_Base):
         self.n_trans = n_trans
         self.squeeze_dims = squeeze_dims
         self._isign = -1
+        self._toep = None
+        self._toeplitz_kernel = None
         self.dtype = np.float32
         self._set_samples(samples)
         G = fine_cells(self.shape, self.eps, self.upsampfac)
@@ -145,6 +147,8 @@ class MRIGB300(_Base):
         (base.py:809-830, finufft.py:150-181)."""
         self._set_samples(new_samples, unsafe=unsafe)
         self._plan.setpts(self._samples_d)
+        self._toep = None
+        self._toeplitz_kernel = None
         self.compute_density(self._density_method)
 
     @property
@@ -195,6 +199,8 @@ class MRIGB300(_Base):
 
     @density.setter
     def density(self, new_density):
+        self._toep = None
+        self._toeplitz_kernel = None
         if new_density is None:
             self._density = None
             return
@@ -212,6 +218,8 @@ class MRIGB300(_Base):
         """Set density compensation (base.py:576-624); True / "pipe" runs the
         pipe estimate on the GPU."""
         kwargs = {}
+        self._toep = None
+        self._toeplitz_kernel = None
         if method is None or method is False:
             self._density = None
             return
@@ -346,10 +354,42 @@ class MRIGB300(_Base):
         return _array.from_tensor(self._safe_squeeze(out), like)
 
     def gram_op(self, data, toeplitz=True):
-        """A^H A x.  Evaluated with one forward and one adjoint transform for
-        either value of ``toeplitz``."""
+        """Gram operator A^H W A x (base.py:315-363).  ``toeplitz=True`` uses
+        the Toeplitz embedding (FFTs and one multiply per coil, no
+        spreading or interpolation); ``toeplitz=False`` one forward and one
+        adjoint transform."""
         self.check_shape(image=data)
-        return self.adj_op(self.op(data))
+        if not toeplitz:
+            return self.adj_op(self.op(data))
+        like = _array.interface_of(data)
+        x = self._img_tensor(data)
+        out = self._gram_device(x)
+        return _array.from_tensor(self._safe_squeeze(out), like)
+
+    def _gram_device(self, x: torch.Tensor) -> torch.Tensor:
+        """Toeplitz Gram of device images ((B, *N) SENSE or (B*C, *N))."""
+        B, C = self.n_batchs, self.n_coils
+        out = torch.empty(self.img_full_shape, dtype=torch.complex64, device=self.device)
+        self._toeplitz().apply(x, self._smaps, out, B, C, self.inv_norm_factor ** 2)
+        return out
+
+    def _toeplitz(self):
+        if self._toep is None:
+            from .plan import ToeplitzKernel
+
+            self._toep = ToeplitzKernel(self._plan, self._density)
+        return self._toep
+
+    def compute_toeplitz_kernel(self):
+        """Compute and set the Toeplitz kernel (base.py:444-449,
+        toeplitz.py:35-96): the real spectrum of A^H W A on the circulant grid
+        (shape 2N where 2N is 2-3-5 smooth), W the density (ones when unset),
+        scaled by 1/norm_factor^2 as in the reference.  Returned as a numpy
+        array."""
+        self._toep = None
+        k = self._toeplitz().kernel() * float(self.inv_norm_factor ** 2)
+        self._toeplitz_kernel = k.cpu().numpy()
+        return self._toeplitz_kernel
 
     # ------------------------------------------------------------ gradients
     def toggle_grad_traj(self):

@@ -181,6 +181,58 @@ class NufftPlan:
         return grad
 
 
+class ToeplitzKernel:
+    """Toeplitz embedding of a plan's Gram operator A^H W A (``gbn_toep``).
+
+    Restates mri-nufft's ``compute_toeplitz_kernel`` / ``apply_toeplitz_kernel``
+    (``src/mrinufft/operators/toeplitz.py:35-96, 193-269``): the real kernel
+    spectrum on a circulant grid of nf >= 2N cells per axis, applied as
+    zero-pad -> FFT -> multiply -> inverse FFT -> crop for every coil of a call.
+    ``weights`` (M,) float32 CUDA tensor or None (ones).
+    """
+
+    def __init__(self, plan: NufftPlan, weights: torch.Tensor | None = None):
+        if plan._coords is None:
+            raise ValueError("the plan has no points")
+        self.plan = plan
+        self.lib = plan.lib
+        self.device = plan.device
+        self._h = ctypes.c_void_p()
+        cols = plan._coords
+        w = None if weights is None else weights.to(self.device, torch.float32).contiguous()
+        _lib.check(
+            self.lib.gbn_toep_create(plan._h, plan.n_samples, _ptr(cols[0]), _ptr(cols[1]),
+                                     _ptr(cols[2]), _ptr(w), ctypes.byref(self._h), plan.stream),
+            "gbn_toep_create",
+        )
+        nf = (ctypes.c_int64 * 3)()
+        _lib.check(self.lib.gbn_toep_info(self._h, nf), "gbn_toep_info")
+        self.grid = tuple(int(v) for v in nf[: plan.ndim])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.gbn_toep_destroy(h)
+            except Exception:  # interpreter shutdown
+                pass
+            self._h = None
+
+    def kernel(self) -> torch.Tensor:
+        """The real kernel spectrum, shape ``grid`` (device, float32)."""
+        out = torch.empty(self.grid, dtype=torch.float32, device=self.device)
+        _lib.check(self.lib.gbn_toep_kernel(self._h, _ptr(out), self.plan.stream), "gbn_toep_kernel")
+        return out
+
+    def apply(self, img, smaps, out, n_batchs, n_coils, scale):
+        _lib.check(
+            self.lib.gbn_toep_apply(self._h, _ptr(img), _ptr(smaps), _ptr(out), n_batchs, n_coils,
+                                    float(scale), self.plan.stream),
+            "gbn_toep_apply",
+        )
+        return out
+
+
 def norm2_f64(x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """sum |x|^2 accumulated in FP64 on the device (returns a 1-element float64 tensor)."""
     if out is None:

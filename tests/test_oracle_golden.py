@@ -83,3 +83,26 @@ def test_odd_size_grids_differ_by_half_shift():
     b = ndft.ndft_type2(k, x, (5, 4), grid="finufft")
     # n0 = -2.5 vs -2
     np.testing.assert_allclose(a / b, np.exp(-2j * np.pi * 0.1 * (-0.5)), rtol=1e-12)
+
+
+TOEP = ["toep2D_w", "toep2D", "toep3D_w"]
+
+
+@pytest.mark.parametrize("name", TOEP)
+def test_toeplitz_oracle_matches_reference(name):
+    # tests/golden/toeplitz_golden.npz: the reference's own compute_toeplitz_kernel
+    # and apply_toeplitz_kernel on its FP64 NDFT backend
+    from pathlib import Path
+
+    from oracle import toeplitz
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "toeplitz_golden.npz")
+    s = g[f"{name}__samples"]
+    shape = tuple(int(v) for v in g[f"{name}__shape"])
+    w = g[f"{name}__weights"]
+    k = toeplitz.toeplitz_kernel(s, shape, w)
+    assert rel_l2(k, g[f"{name}__kernel"]) < 1e-12
+    x = g[f"{name}__img"]
+    assert rel_l2(toeplitz.apply_toeplitz(x, k), g[f"{name}__gram"]) < 1e-12
+    ref = NDFTOperator(s, shape, density=w)
+    assert rel_l2(ref.adj(ref.op(x)), g[f"{name}__gram"]) < 1e-12
