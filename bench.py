@@ -75,7 +75,8 @@ class ClockSampler:
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+              "utilization.gpu")
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
@@ -104,7 +105,7 @@ class ClockSampler:
         self.f.flush()
         rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
-        sm, smax, reasons = [], [], set()
+        sm, smax, util, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
             try:
@@ -112,6 +113,10 @@ class ClockSampler:
                 smax.append(float(r[1]))
             except (ValueError, IndexError):
                 continue
+            try:
+                util.append(float(r[8]))
+            except (ValueError, IndexError):
+                pass
             for n, v in zip(names, r[4:8]):
                 if v.strip().lower() == "active":
                     reasons.add(n)
@@ -120,6 +125,7 @@ class ClockSampler:
             "sm_max_mhz": max(smax) if smax else None,
             "reasons": sorted(reasons),
             "samples": len(sm),
+            "gpu_util_pct": statistics.median(util) if util else None,
         }
 
 
@@ -547,8 +553,9 @@ def c5_templates(dev):
         op = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps, squeeze_dims=False, device=dev.index)
         y = op.op(torch.from_numpy(x).to(dev)).reshape(C, -1)
         y = y + 0.01 * torch.randn_like(y)
+        # k-space arrives in pinned host memory (copied to the device per request)
         out.append({"key": key, "prob": prob, "samples": traj, "shape": shape, "smaps": smaps,
-                    "kspace": y.cpu().numpy()})
+                    "kspace": y.cpu().pin_memory()})
         del op
     return out
 
@@ -574,7 +581,8 @@ def run_c5(args):
         for i, (k, a) in enumerate(zip(picks, arrivals)):
             t = tpl[k]
             reqs.append(ReconRequest(rid=i, samples=t["samples"], shape=t["shape"], kspace=t["kspace"],
-                                     smaps=t["smaps"], seed=i, traj_key=t["key"], arrival=float(a)))
+                                     smaps=t["smaps"], seed=i, traj_key=t["key"], smaps_key=t["key"],
+                                     arrival=float(a)))
         return reqs
 
     # warm the plan pools and kernels
@@ -591,11 +599,16 @@ def run_c5(args):
     nsat = args.saturated
     sat_reqs = make(nsat, np.zeros(nsat))
     srv2 = ReconServer(hbm_budget_bytes=150e9, max_active=32)
+    sampler = ClockSampler(0)
+    sampler.start()
     t0 = time.perf_counter()
     srv2.run(sat_reqs, realtime=False)
     served_s = time.perf_counter() - t0
+    served_clk = sampler.stop()
     # plain per-call backend on the same requests (host-synchronised CG loop)
     ops = {}
+    sampler = ClockSampler(0)
+    sampler.start()
     t0 = time.perf_counter()
     for r in sat_reqs:
         key = r.traj_key
@@ -604,9 +617,10 @@ def run_c5(args):
             ops[key] = pkg.MRIGB300(t["samples"], t["shape"], n_coils=t["smaps"].shape[0],
                                     smaps=t["smaps"], device=0)
         np.random.seed(r.seed)
-        ops[key].pinv_solver(torch.from_numpy(r.kspace).to(dev), optim="cg", max_iter=10)
+        ops[key].pinv_solver(r.kspace.to(dev, non_blocking=True), optim="cg", max_iter=10)
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
+    plain_clk = sampler.stop()
     line = {
         "metric": "served CG reconstructions: p50/p99 latency (ms) and recon/s",
         "value": nsat / served_s, "unit": "recon/s", "n_gpus": 1, "steps": nsat, "warmup": len(tpl) * 2,
@@ -619,7 +633,8 @@ def run_c5(args):
         "stream": stream,
         "saturated": {"requests": nsat, "served_recon_per_s": nsat / served_s,
                       "plain_per_call_recon_per_s": nsat / plain_s,
-                      "speedup": plain_s / served_s},
+                      "speedup": plain_s / served_s,
+                      "served_clocks": served_clk, "plain_clocks": plain_clk},
     }
     print(json.dumps(line), flush=True)
 

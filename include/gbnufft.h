@@ -217,6 +217,22 @@ int gbn_toep_apply(gbn_toep toep, const void* img, const void* smaps, void* out,
 int gbn_toep_destroy(gbn_toep toep);
 
 /*
+ * Served-solver steps on the Toeplitz Gram, one call per iteration (no
+ * reference counterpart as single calls; they fuse the loop bodies of
+ * extras/optim.py:859-893 and base.py:1196-1212 for device-resident state):
+ *   gbn_toep_cg_iter: grad_new = A^H A image - rhs (rhs = A^H y, the same
+ *     image layout; scale = 1/norm^2), then the dots of gbn_cg_update's
+ *     state[0..6] and the update of gbn_cg_update.
+ *   gbn_toep_power_iter: x_new = A^H W A x (one image, no maps), then
+ *     state[0] = |x_new|^2 and the step of gbn_power_step.
+ */
+int gbn_toep_cg_iter(gbn_toep toep, void* image, const void* smaps, const void* rhs, void* grad,
+                     void* grad_new, void* velocity, double* state, const float* lipschitz, int B,
+                     int C, float scale, float tol, gbn_stream stream);
+int gbn_toep_power_iter(gbn_toep toep, void* x, void* x_new, double* state, float* lipschitz,
+                        float scale, gbn_stream stream);
+
+/*
  * Stage timing.  gbn_profile(plan, 1) clears the counters and records a pair
  * of CUDA events on the launch stream around every launch of a stage;
  * gbn_profile(plan, 0) stops recording.  gbn_profile_read waits for the

@@ -62,7 +62,8 @@ def to_tensor(x, device: torch.device, dtype: torch.dtype) -> torch.Tensor:
     if t.dtype != dtype:
         t = t.to(dtype)
     if t.device != device:
-        t = t.to(device, non_blocking=False)
+        # pinned host memory copies asynchronously on the current stream
+        t = t.to(device, non_blocking=t.device.type == "cpu" and t.is_pinned())
     return t.contiguous()
 
 

@@ -1130,6 +1130,40 @@ namespace {
 void chk(int rc) {
   if (rc != GBN_OK) throw Fail{rc};  // the message is already set
 }
+
+// A^H W A x by the Toeplitz embedding for every batch item and coil: per coil
+// pass zero-pad (x * s_c), FFT, multiply by K, inverse FFT, crop with the
+// conj(s_c) coil sum, times scale / prod(nf); `accumulate` adds every pass
+// to what `out` holds.
+void toep_apply(gbn_toep t, const void* img, const void* smaps, void* out, int B, int C,
+                float scale, bool accumulate, cudaStream_t st) {
+  gbn_plan p = t->inner;
+  check_counts(B, C);
+  if (!img || !out) fail(GBN_ERR_ARG, "null image pointer");
+  const float2* x = static_cast<const float2*>(img);
+  const float2* s = static_cast<const float2*>(smaps);
+  float2* o = static_cast<float2*>(out);
+  const Geom& g = p->g;
+  const float sc = (float)((double)scale / (double)g.G);  // inverse-FFT normalisation
+  for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
+    PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
+                   : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
+    pa.dec[0] = pa.dec[1] = pa.dec[2] = nullptr;
+    run_pad(p, pa, st);
+    p->exec_fft(T, p->fine, -1, st, 1);
+    {
+      Span span(p, GBN_STAGE_KMUL, st);
+      ck(launch_kmul(p->fine, t->K, g.G, T, st), "Toeplitz multiply");
+      p->launches++;
+    }
+    p->exec_fft(T, p->fine, +1, st, 2);
+    CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, o + (int64_t)b * g.Nimg, T,
+                                accumulate || c0 > 0, sc)
+                    : crop_args(p, nullptr, o + (int64_t)c0 * g.Nimg, T, accumulate, sc);
+    ca.dec[0] = ca.dec[1] = ca.dec[2] = nullptr;
+    run_crop(p, ca, st);
+  });
+}
 }  // namespace
 
 extern "C" {
@@ -1219,33 +1253,51 @@ int gbn_toep_apply(gbn_toep t, const void* img, const void* smaps, void* out, in
     g_err = "null Toeplitz handle";
     return GBN_ERR_ARG;
   }
-  gbn_plan p = t->inner;
-  return guarded(p, [&] {
-    check_counts(B, C);
-    if (!img || !out) fail(GBN_ERR_ARG, "null image pointer");
+  return guarded(t->inner, [&] {
+    toep_apply(t, img, smaps, out, B, C, scale, false, reinterpret_cast<cudaStream_t>(stream));
+  });
+}
+
+int gbn_toep_cg_iter(gbn_toep t, void* image, const void* smaps, const void* rhs, void* grad,
+                     void* grad_new, void* velocity, double* state, const float* lipschitz, int B,
+                     int C, float scale, float tol, gbn_stream stream) {
+  if (!t) {
+    g_err = "null Toeplitz handle";
+    return GBN_ERR_ARG;
+  }
+  return guarded(t->inner, [&] {
+    if (!image || !rhs || !grad || !grad_new || !velocity || !state || !lipschitz)
+      fail(GBN_ERR_ARG, "null pointer");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const float2* x = static_cast<const float2*>(img);
-    const float2* s = static_cast<const float2*>(smaps);
-    float2* o = static_cast<float2*>(out);
-    const Geom& g = p->g;
-    const float sc = (float)((double)scale / (double)g.G);  // inverse-FFT normalisation
-    for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
-      PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
-                     : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
-      pa.dec[0] = pa.dec[1] = pa.dec[2] = nullptr;
-      run_pad(p, pa, st);
-      p->exec_fft(T, p->fine, -1, st, 1);
-      {
-        Span span(p, GBN_STAGE_KMUL, st);
-        ck(launch_kmul(p->fine, t->K, g.G, T, st), "Toeplitz multiply");
-        p->launches++;
-      }
-      p->exec_fft(T, p->fine, +1, st, 2);
-      CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, o + (int64_t)b * g.Nimg, T, c0 > 0, sc)
-                      : crop_args(p, nullptr, o + (int64_t)c0 * g.Nimg, T, 0, sc);
-      ca.dec[0] = ca.dec[1] = ca.dec[2] = nullptr;
-      run_crop(p, ca, st);
-    });
+    const Geom& g = t->inner->g;
+    const int64_t n = (int64_t)B * (smaps ? 1 : C) * g.Nimg;
+    float2* gn = static_cast<float2*>(grad_new);
+    ck(launch_neg_copy(static_cast<const float2*>(rhs), gn, n, st), "CG gradient");
+    toep_apply(t, image, smaps, gn, B, C, scale, true, st);
+    ck(launch_cg_dots(gn, static_cast<const float2*>(grad), n, state, st), "CG dots");
+    ck(launch_cg_update(n, gn, static_cast<float2*>(grad), static_cast<float2*>(velocity),
+                        static_cast<float2*>(image), state, lipschitz, tol, st),
+       "CG update");
+    t->inner->launches += 4;
+  });
+}
+
+int gbn_toep_power_iter(gbn_toep t, void* x, void* x_new, double* state, float* lipschitz,
+                        float scale, gbn_stream stream) {
+  if (!t) {
+    g_err = "null Toeplitz handle";
+    return GBN_ERR_ARG;
+  }
+  return guarded(t->inner, [&] {
+    if (!x || !x_new || !state || !lipschitz) fail(GBN_ERR_ARG, "null pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t n = t->inner->g.Nimg;
+    toep_apply(t, x, nullptr, x_new, 1, 1, scale, false, st);
+    ck(launch_norm2(static_cast<const float2*>(x_new), n, state, st), "power norm");
+    ck(launch_power_step(n, static_cast<const float2*>(x_new), static_cast<float2*>(x), state,
+                         lipschitz, st),
+       "power step");
+    t->inner->launches += 3;
   });
 }
 

@@ -277,6 +277,61 @@ static unsigned elem_blocks(int64_t n) {
   return (unsigned)(b < 1216 ? (b < 1 ? 1 : b) : 1216);
 }
 
+__global__ void neg_copy_kernel(const float2* __restrict__ in, float2* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    out[i] = make_float2(-v.x, -v.y);
+  }
+}
+
+__global__ void cg_dots_kernel(const float2* __restrict__ gn, const float2* __restrict__ g,
+                               int64_t n, double* st) {
+  __shared__ double sm[7][32];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = gn[i], b = g[i];
+    const double ar = a.x, ai = a.y, br = b.x, bi = b.y;
+    acc[0] += ar * ar - ai * ai;  // dotu(gn, gn) (non-conjugating)
+    acc[1] += 2.0 * ar * ai;
+    acc[2] += ar * br - ai * bi;  // dotu(gn, g)
+    acc[3] += ar * bi + ai * br;
+    acc[4] += br * br - bi * bi;  // dotu(g, g)
+    acc[5] += 2.0 * br * bi;
+    acc[6] += ar * ar + ai * ai;  // |gn|^2
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    double v = warp_sum(acc[k]);
+    if (lane == 0) sm[k][wid] = v;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      double v = lane < (int)(blockDim.x >> 5) ? sm[k][lane] : 0.0;
+      v = warp_sum(v);
+      if (lane == 0) atomicAdd(&st[k], v);
+    }
+  }
+}
+
+cudaError_t launch_neg_copy(const float2* in, float2* out, int64_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  neg_copy_kernel<<<elem_blocks(n), 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cg_dots(const float2* gnew, const float2* grad, int64_t n, double* st,
+                           cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(st, 0, 7 * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  cg_dots_kernel<<<reduce_blocks(n), 256, 0, s>>>(gnew, grad, n, st);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cg_update(int64_t n, const float2* gnew, float2* grad, float2* vel, float2* img,
                              double* st, const float* L, float tol, cudaStream_t s) {
   cg_update_kernel<<<elem_blocks(n), 256, 0, s>>>(n, gnew, grad, vel, img, st, L, tol);

@@ -23,7 +23,7 @@ struct CropArgs {
   const float* dec[3];  // 1/phihat per axis (null: 1)
   float2* out;          // SENSE: one image; calibrationless: ntr images
   int ntr;
-  int accumulate;       // SENSE: out += result
+  int accumulate;       // out += result
   float scale;
 };
 
@@ -123,7 +123,13 @@ __device__ __forceinline__ void crop_body(const CropArgs& a, const int64_t idx) 
   } else {
     for (int c = 0; c < a.ntr; ++c) {
       float2 v = a.fine[(int64_t)c * g.G + mlin];
-      a.out[(int64_t)c * g.Nimg + idx] = make_float2(v.x * f, v.y * f);
+      float2 r = make_float2(v.x * f, v.y * f);
+      if (a.accumulate) {
+        float2 o = a.out[(int64_t)c * g.Nimg + idx];
+        r.x += o.x;
+        r.y += o.y;
+      }
+      a.out[(int64_t)c * g.Nimg + idx] = r;
     }
   }
 }
@@ -136,6 +142,12 @@ cudaError_t launch_kmul(float2* fine, const float* K, int64_t G, int ntr, cudaSt
 cudaError_t launch_toep_place(const Geom& gt, const float2* psf, float2* dst, cudaStream_t st);
 cudaError_t launch_real_part(const float2* src, float* dst, int64_t n, float scale, cudaStream_t st);
 cudaError_t launch_fill_weights(const float* w, float2* out, int64_t M, cudaStream_t st);
+// out = -in (n complex values)
+cudaError_t launch_neg_copy(const float2* in, float2* out, int64_t n, cudaStream_t st);
+// CG reductions in one pass (FP64): st[0..1] = dotu(gn, gn), st[2..3] =
+// dotu(gn, g), st[4..5] = dotu(g, g), st[6] = |gn|^2; st[7] is kept
+cudaError_t launch_cg_dots(const float2* gnew, const float2* grad, int64_t n, double* st,
+                           cudaStream_t s);
 cudaError_t launch_pad(const PadArgs& a, cudaStream_t st);
 cudaError_t launch_crop(const CropArgs& a, cudaStream_t st);
 cudaError_t launch_norm2(const float2* x, int64_t n, double* out, cudaStream_t st);

@@ -19,7 +19,14 @@ and coil counts as they arrive:
 * no host synchronisation inside a solve: the power-method normalisation,
   the CG step (Polak-Ribiere beta with numpy's complex ``max(0, beta)``, the
   ``tol`` early exit) and their FP64 reductions run on the device
-  (``gbn_power_step``, ``gbn_cg_update``, ``gbn_dotu_f64``, ``gbn_norm2_f64``).
+  (``gbn_power_step``, ``gbn_cg_update``, ``gbn_dotu_f64``, ``gbn_norm2_f64``);
+* FFT-only iterations: the power method and the CG gradients use the
+  Toeplitz embedding of the Gram operator (``gbn_toep_*``; A^H W A x as a
+  circulant convolution on a 2N grid), so an iteration runs FFTs and one
+  multiply per coil instead of a spread and an interpolation.  The CG
+  gradient A^H A x - A^H y takes A^H y from one adjoint transform at the
+  start.  The Toeplitz kernel of a trajectory is built once and pooled with
+  its sorted plan.
 
 Each result equals the same request run alone (and ``MRIGB300.pinv_solver``
 with the same power-method start vector) up to float rounding.
@@ -30,6 +37,7 @@ from __future__ import annotations
 import ctypes
 import time
 from collections import defaultdict, deque
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -55,6 +63,7 @@ class ReconRequest:
     tol: float = 1e-4
     seed: int = 0             # power-method start vector
     traj_key: object = None   # requests with equal keys share a sorted trajectory
+    smaps_key: object = None  # requests with equal keys share resident coil maps
     arrival: float = 0.0
     result: torch.Tensor = None
     t_admit: float = None
@@ -68,30 +77,46 @@ class ReconRequest:
 
 def start_vector(shape, seed):
     """1j * U[0,1) + U[0,1), the start vector of the GPU backends'
-    ``get_lipschitz_cst`` (cufinufft.py:1265-1266), from a seeded generator."""
+    ``get_lipschitz_cst`` (cufinufft.py:1265-1266), from a seeded generator
+    (imaginary part drawn first, both parts rounded to float32)."""
     rs = np.random.RandomState(seed)
-    x = 1j * rs.random_sample(shape).astype(np.complex64)
-    x += rs.random_sample(shape).astype(np.complex64)
+    x = np.empty(shape, np.complex64)
+    x.imag = rs.random_sample(shape)
+    x.real = rs.random_sample(shape)
     return x
 
 
 def request_bytes(shape, M, C, eps=1e-6):
     """Device bytes of one admitted request: plan (fine grids, sort tables),
-    coil maps, k-space, CG / power-method vectors."""
+    Toeplitz kernel and its grids, coil maps, k-space, CG / power-method
+    vectors."""
     G = fine_cells(shape, eps)
     N = int(np.prod(shape))
     d = len(shape)
     plan = 8 * C * G + M * (12 + 4 * d) + 8 * C * M
+    toep = 8 * C * G + 4 * G
     data = 8 * C * N + 8 * C * M + 4 * M
-    state = 8 * N * 7
-    return int(plan + data + state)
+    state = 8 * N * 8
+    return int(plan + toep + data + state)
+
+
+class _PlanSet:
+    """A sorted trajectory: the NUFFT plan and the Toeplitz embedding of its
+    unweighted Gram operator."""
+
+    def __init__(self, plan):
+        from .plan import ToeplitzKernel
+
+        self.plan = plan
+        self.toep = ToeplitzKernel(plan, None)
 
 
 class _Solve:
     """Device state and unit generator of one admitted request."""
 
-    def __init__(self, server, req, plan, stream):
-        self.server, self.req, self.plan, self.stream = server, req, plan, stream
+    def __init__(self, server, req, pset, stream):
+        self.server, self.req, self.stream = server, req, stream
+        self.pset, self.plan = pset, pset.plan
         self.dev = server.device
         self.lib = server.lib
         shape = tuple(int(v) for v in req.shape)
@@ -100,11 +125,11 @@ class _Solve:
         self.C = C
         with torch.cuda.stream(stream):
             self.y = _array.to_tensor(req.kspace, self.dev, torch.complex64).reshape(C, -1)
-            self.smaps = (None if req.smaps is None
-                          else _array.to_tensor(req.smaps, self.dev, torch.complex64).reshape(C, *shape))
+            self.smaps = None if req.smaps is None else server._smaps_of(req, C, shape)
             self.dens = (None if req.density is None
                          else _array.to_tensor(req.density, self.dev, torch.float32).reshape(-1))
-            self.x0 = torch.from_numpy(start_vector(shape, req.seed)).to(self.dev, non_blocking=True)
+            x0 = req._x0.result() if getattr(req, "_x0", None) is not None else start_vector(shape, req.seed)
+            self.x0 = torch.from_numpy(x0).to(self.dev)
         self.M = self.y.shape[1]
         self.scale = 1.0 / float(np.sqrt(np.prod(shape) * 2 ** len(shape)))
         self.bytes = request_bytes(shape, self.M, C, server.eps)
@@ -126,6 +151,13 @@ class _Solve:
         f32 = dict(dtype=torch.float32, device=dev)
         c64 = dict(dtype=torch.complex64, device=dev)
         f64 = dict(dtype=torch.float64, device=dev)
+        scale2 = self.scale * self.scale
+        toep = self.pset.toep
+        toep_w = toep
+        if self.dens is not None:
+            from .plan import ToeplitzKernel
+
+            toep_w = ToeplitzKernel(plan, self.dens)  # A^H D A of the power method
         L = torch.zeros(1, **f32)
         pst = torch.zeros(4, **f64)
         x = torch.empty((1, *shape), **c64)
@@ -137,11 +169,7 @@ class _Solve:
                  "power step")
         yield
         for _ in range(10):
-            plan.op(x, None, ktmp, 1, 1, self.scale)
-            plan.adj(ktmp, self.dens, None, xn, 1, 1, self.scale)
-            self._ck(self.lib.gbn_norm2_f64(_ptr(xn), n, _ptr(pst), self._st()), "norm2")
-            self._ck(self.lib.gbn_power_step(n, _ptr(xn), _ptr(x), _ptr(pst), _ptr(L), self._st()),
-                     "power step")
+            toep_w.power_iter(x, xn, pst, L, scale2)
             yield
         self.L = L
         # -- start image: scaled density-compensated adjoint (optim.py:151-165)
@@ -157,24 +185,22 @@ class _Solve:
             self._ck(self.lib.gbn_scale_ratio(nimg, _ptr(image), _ptr(nrm[0:1]), _ptr(nrm[1:2]),
                                               self._st()), "scale")
             yield
-        # -- CG iterations without density (optim.py:838-842)
+        # -- CG iterations without density (optim.py:838-842); the gradient
+        # A^H (A x - y) = A^H A x - A^H y with A^H y from one adjoint
+        rhs = torch.empty(img_shape, **c64)
+        plan.adj(y, None, self.smaps, rhs, 1, C, self.scale)
         grad = torch.empty(img_shape, **c64)
         gnew = torch.empty(img_shape, **c64)
         xin = image.reshape(1 if sense else C, *shape)
-        plan.dc(xin, y, None, self.smaps, grad, 1, C, self.scale)
+        toep.apply(xin, self.smaps, grad, 1, C, scale2)
+        grad -= rhs
         velocity = grad / L
         image -= velocity
         st = torch.zeros(8, **f64)
         yield
+        tol = float(self.req.tol)
         for _ in range(self.req.max_iter):
-            plan.dc(xin, y, None, self.smaps, gnew, 1, C, self.scale)
-            s = self._st()
-            self._ck(self.lib.gbn_dotu_f64(_ptr(gnew), _ptr(gnew), nimg, 0, _ptr(st[0:2]), s), "dot")
-            self._ck(self.lib.gbn_dotu_f64(_ptr(gnew), _ptr(grad), nimg, 0, _ptr(st[2:4]), s), "dot")
-            self._ck(self.lib.gbn_dotu_f64(_ptr(grad), _ptr(grad), nimg, 0, _ptr(st[4:6]), s), "dot")
-            self._ck(self.lib.gbn_norm2_f64(_ptr(gnew), nimg, _ptr(st[6:7]), s), "norm2")
-            self._ck(self.lib.gbn_cg_update(nimg, _ptr(gnew), _ptr(grad), _ptr(velocity), _ptr(image),
-                                            _ptr(st), _ptr(L), float(self.req.tol), s), "cg update")
+            toep.cg_iter(image, self.smaps, rhs, grad, gnew, velocity, st, L, 1, C, scale2, tol)
             yield
         self.image = image
         self.event = torch.cuda.Event()
@@ -205,6 +231,8 @@ class ReconServer:
         self.done = []
         self.used = 0
         self.plans = defaultdict(list)   # (traj key, shape, coils) -> free sorted plans
+        self.smaps_cache = {}            # smaps key -> resident coil maps
+        self.rng_pool = ThreadPoolExecutor(max_workers=4)
         self.plan_bytes = 0
         self.streams = [torch.cuda.Stream(self.device) for _ in range(self.max_active)]
         self.free_streams = list(range(self.max_active))
@@ -214,7 +242,21 @@ class ReconServer:
         return time.perf_counter() - self.t0
 
     def submit(self, req: ReconRequest):
+        # the power-method start vector is drawn on a host thread while the
+        # request waits; admission takes requests whose vector is ready
+        req._x0 = self.rng_pool.submit(start_vector, tuple(int(v) for v in req.shape), req.seed)
         self.queue.append(req)
+
+    def _smaps_of(self, req, C, shape):
+        """Device coil maps of a request; maps with a ``smaps_key`` stay
+        resident for later requests with the same key."""
+        if req.smaps_key is not None and req.smaps_key in self.smaps_cache:
+            return self.smaps_cache[req.smaps_key]
+        t = _array.to_tensor(req.smaps, self.device, torch.complex64).reshape(C, *shape)
+        if req.smaps_key is not None:
+            self.smaps_cache[req.smaps_key] = t
+            self.plan_bytes += t.numel() * 8
+        return t
 
     def _acquire_plan(self, req, stream):
         shape = tuple(int(v) for v in req.shape)
@@ -227,12 +269,15 @@ class ReconServer:
             s = proper_trajectory(req.samples, "pi")
             k = _array.to_tensor(s, self.device, torch.float32).reshape(-1, len(shape))
             plan.setpts(k)
+            pset = _PlanSet(plan)
         self.plan_bytes += plan.device_bytes
-        return key, plan
+        return key, pset
 
     def _admit(self):
         while self.queue and self.free_streams:
             req = self.queue[0]
+            if not req._x0.done():
+                break
             need = request_bytes(tuple(req.shape), int(np.asarray(req.kspace.shape)[-1]),
                                  req.n_coils, self.eps)
             if (self.active or self.finishing) and self.used + need > self.budget:
@@ -240,8 +285,8 @@ class ReconServer:
             self.queue.popleft()
             si = self.free_streams.pop()
             stream = self.streams[si]
-            key, plan = self._acquire_plan(req, stream)
-            solve = _Solve(self, req, plan, stream)
+            key, pset = self._acquire_plan(req, stream)
+            solve = _Solve(self, req, pset, stream)
             solve.key, solve.si = key, si
             self.used += solve.bytes
             req.t_admit = self.now()
@@ -255,7 +300,7 @@ class ReconServer:
                 s.req.lipschitz = s.L
                 s.req.t_done = self.now()
                 self.used -= s.bytes
-                self.plans[s.key].append(s.plan)
+                self.plans[s.key].append(s.pset)
                 self.free_streams.append(s.si)
                 self.done.append(s.req)
             else:
@@ -291,7 +336,7 @@ class ReconServer:
                     time.sleep(max(0.0, min(poll_s * 10, pending[0].arrival - now)))
                 continue
             self.tick()
-            if not self.active and self.finishing:
+            if not self.active:
                 time.sleep(poll_s)
         torch.cuda.synchronize(self.device)
         return self.done
