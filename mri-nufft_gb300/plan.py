@@ -233,20 +233,22 @@ class ToeplitzKernel:
         return out
 
     def cg_iter(self, image, smaps, rhs, grad, grad_new, velocity, state, lipschitz, n_batchs,
-                n_coils, scale, tol):
-        """One CG iteration with the gradient A^H A x - rhs (``gbn_toep_cg_iter``)."""
+                n_coils, scale, tol, stream=None):
+        """One CG iteration with the gradient A^H A x - rhs (``gbn_toep_cg_iter``);
+        ``stream``: a ctypes stream handle (default: torch's current stream)."""
         _lib.check(
             self.lib.gbn_toep_cg_iter(self._h, _ptr(image), _ptr(smaps), _ptr(rhs), _ptr(grad),
                                       _ptr(grad_new), _ptr(velocity), _ptr(state), _ptr(lipschitz),
-                                      n_batchs, n_coils, float(scale), float(tol), self.plan.stream),
+                                      n_batchs, n_coils, float(scale), float(tol),
+                                      self.plan.stream if stream is None else stream),
             "gbn_toep_cg_iter",
         )
 
-    def power_iter(self, x, x_new, state, lipschitz, scale):
+    def power_iter(self, x, x_new, state, lipschitz, scale, stream=None):
         """One power-method iteration on A^H W A (``gbn_toep_power_iter``)."""
         _lib.check(
             self.lib.gbn_toep_power_iter(self._h, _ptr(x), _ptr(x_new), _ptr(state), _ptr(lipschitz),
-                                         float(scale), self.plan.stream),
+                                         float(scale), self.plan.stream if stream is None else stream),
             "gbn_toep_power_iter",
         )
 

@@ -133,11 +133,14 @@ class _Solve:
         self.M = self.y.shape[1]
         self.scale = 1.0 / float(np.sqrt(np.prod(shape) * 2 ** len(shape)))
         self.bytes = request_bytes(shape, self.M, C, server.eps)
+        self._sth = None
         self.gen = self._units()
         self.event = None
 
     def _st(self):
-        return ctypes.c_void_p(self.stream.cuda_stream)
+        if self._sth is None:
+            self._sth = ctypes.c_void_p(self.stream.cuda_stream)
+        return self._sth
 
     def _ck(self, status, what):
         _lib.check(status, what)
@@ -168,8 +171,9 @@ class _Solve:
         self._ck(self.lib.gbn_power_step(n, _ptr(self.x0), _ptr(x), _ptr(pst), _ptr(L), self._st()),
                  "power step")
         yield
+        sth = self._st()
         for _ in range(10):
-            toep_w.power_iter(x, xn, pst, L, scale2)
+            toep_w.power_iter(x, xn, pst, L, scale2, sth)
             yield
         self.L = L
         # -- start image: scaled density-compensated adjoint (optim.py:151-165)
@@ -200,7 +204,7 @@ class _Solve:
         yield
         tol = float(self.req.tol)
         for _ in range(self.req.max_iter):
-            toep.cg_iter(image, self.smaps, rhs, grad, gnew, velocity, st, L, 1, C, scale2, tol)
+            toep.cg_iter(image, self.smaps, rhs, grad, gnew, velocity, st, L, 1, C, scale2, tol, sth)
             yield
         self.image = image
         self.event = torch.cuda.Event()
@@ -241,6 +245,27 @@ class ReconServer:
     def now(self):
         return time.perf_counter() - self.t0
 
+    def prewarm(self, requests, per_key=None):
+        """Build the resident sorted plans and Toeplitz kernels that
+        ``requests`` will need before they arrive, so that admission never
+        sorts a trajectory on a request's critical path: ``per_key`` plan sets
+        per trajectory key, by default the key's share of the slots (its
+        share of ``requests`` times ``max_active``, plus 2)."""
+        counts, first = defaultdict(int), {}
+        for r in requests:
+            shape = tuple(int(v) for v in r.shape)
+            key = (r.traj_key if r.traj_key is not None else ("rid", r.rid), shape, r.n_coils)
+            counts[key] += 1
+            first.setdefault(key, r)
+        n = max(1, len(requests))
+        for key, r in first.items():
+            want = (int(per_key) if per_key is not None
+                    else min(self.max_active, int(np.ceil(self.max_active * counts[key] / n)) + 2))
+            with torch.cuda.stream(self.streams[0]):
+                while len(self.plans[key]) < want:
+                    self.plans[key].append(self._acquire_plan(r, self.streams[0], fresh=True)[1])
+        torch.cuda.synchronize(self.device)
+
     def submit(self, req: ReconRequest):
         # the power-method start vector is drawn on a host thread while the
         # request waits; admission takes requests whose vector is ready
@@ -258,11 +283,11 @@ class ReconServer:
             self.plan_bytes += t.numel() * 8
         return t
 
-    def _acquire_plan(self, req, stream):
+    def _acquire_plan(self, req, stream, fresh=False):
         shape = tuple(int(v) for v in req.shape)
         key = (req.traj_key if req.traj_key is not None else ("rid", req.rid), shape, req.n_coils)
         pool = self.plans[key]
-        if pool:
+        if pool and not fresh:
             return key, pool.pop()
         with torch.cuda.stream(stream):
             plan = NufftPlan(shape, eps=self.eps, ntrans=req.n_coils, device=self.device.index)
