@@ -56,10 +56,11 @@ def parse():
     p.add_argument("--rate", type=float, default=50.0, help="c5: Poisson arrival rate (req/s)")
     p.add_argument("--saturated", type=int, default=300,
                    help="c5: requests of the saturated served-vs-plain comparison")
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "gram"],
                    help="c2: 3D 16-coil SENSE (default line); c1: 2D 256^2 single-coil radial; "
                         "c3: 32 uneven 2D instances, batched graph-captured launch vs per-call "
-                        "loop; c4: differentiable forward+backward; c5: served CG stream")
+                        "loop; c4: differentiable forward+backward; c5: served CG stream; gram: Toeplitz "
+                        "Gram operator vs op+adj")
     return p.parse_args()
 
 
@@ -525,6 +526,69 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gram(args):
+    """Toeplitz Gram operator on the 3D workload: A^H A x for 16 coils by the
+    Toeplitz embedding (pad, FFT, multiply, inverse FFT, crop) against one
+    forward plus one adjoint NUFFT."""
+    import torch
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    __graft_entry__.build()
+    pkg = __graft_entry__.import_package()
+    from mrinufft_gb300 import workloads
+
+    traj, shape, img, smaps = workloads.config2(args.spokes, args.samples, args.coils, args.size)
+    M, C = traj.shape[0], smaps.shape[0]
+    op = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps, squeeze_dims=False)
+    x = torch.from_numpy(img).to(dev).reshape(1, *shape)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    toep = op._toeplitz()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    toep.profile(True)
+    ms_toep = timed(lambda: op._gram_device(x))
+    stages = {s: toep.profile_read(s) for s in ("pad", "fft", "kmul", "crop")}
+    toep.profile(False)
+    ms_nufft = timed(lambda: op._adj_device(op._op_device(x)))
+    G = int(np.prod(toep.grid))
+    kmul_ms = stages["kmul"][0] / max(1, stages["kmul"][1])
+    kmul_bytes = 16 * op._ntrans * G + 4 * G
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    peak = float(json.loads(peaks_path.read_text())["hbm_gbs"]) if peaks_path.exists() else 6800.0
+    line = {
+        "metric": "Gram operator A^H A x Msamples*coil/s equivalent (Toeplitz embedding)",
+        "value": M * C / (ms_toep / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_toep, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (seeded kooshball, ellipsoid phantom, Gaussian coil maps)",
+        "config": {"workload": f"3D SENSE Gram, {shape[0]}^3 image, {C} coils, kooshball "
+                               f"{args.spokes}x{args.samples}", "circulant_grid": list(toep.grid),
+                   "kernel_build_s": build_s},
+        "nufft_op_adj_ms": ms_nufft, "speedup_vs_nufft": ms_nufft / ms_toep,
+        "stage_ms_per_step": {s: v[0] / args.steps for s, v in stages.items()},
+        "roofline": {"bound": "hbm", "kernel": "kmul", "achieved": kmul_bytes / (kmul_ms / 1e3) / 1e9,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": kmul_bytes / (kmul_ms / 1e3) / 1e9 / peak,
+                     "algorithmic_bytes_per_launch": kmul_bytes},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def c5_templates(dev):
     """Request templates of the served mix: 2D 256^2 radial 256x512 with 8, 16,
     24 or 32 coils (70 %), 2D 384^2 spiral 32x4096 with 16 coils (20 %), 3D
@@ -655,6 +719,8 @@ def main():
         run_c3(args)
     elif args.workload == "c4":
         run_c4(args)
+    elif args.workload == "gram":
+        run_gram(args)
     elif args.workload == "c5":
         run_c5(args)
     else:

@@ -215,6 +215,9 @@ int gbn_toep_kernel(gbn_toep toep, float* dst, gbn_stream stream);
 int gbn_toep_apply(gbn_toep toep, const void* img, const void* smaps, void* out, int B, int C,
                    float scale, gbn_stream stream);
 int gbn_toep_destroy(gbn_toep toep);
+/* The handle's circulant-grid plan (owned by the handle), for gbn_profile /
+ * gbn_profile_read of its pad / FFT / multiply / crop stages. */
+int gbn_toep_plan(gbn_toep toep, gbn_plan* out);
 
 /*
  * Served-solver steps on the Toeplitz Gram, one call per iteration (no

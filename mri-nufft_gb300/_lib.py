@@ -64,6 +64,7 @@ SIGNATURES = {
     "gbn_toep_kernel": (_c_int, [_vp, _vp, _vp]),
     "gbn_toep_apply": (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _vp]),
     "gbn_toep_destroy": (_c_int, [_vp]),
+    "gbn_toep_plan": (_c_int, [_vp, ctypes.POINTER(_vp)]),
     "gbn_toep_cg_iter": (
         _c_int,
         [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_flt, _c_flt, _vp],

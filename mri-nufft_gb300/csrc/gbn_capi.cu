@@ -1301,6 +1301,15 @@ int gbn_toep_power_iter(gbn_toep t, void* x, void* x_new, double* state, float* 
   });
 }
 
+int gbn_toep_plan(gbn_toep t, gbn_plan* out) {
+  if (!t || !out) {
+    g_err = "null argument";
+    return GBN_ERR_ARG;
+  }
+  *out = t->inner;
+  return GBN_OK;
+}
+
 int gbn_toep_destroy(gbn_toep t) {
   delete t;
   return GBN_OK;

@@ -218,6 +218,23 @@ class ToeplitzKernel:
                 pass
             self._h = None
 
+    def profile(self, enable: bool = True):
+        """Stage timing of the circulant-grid plan (see NufftPlan.profile)."""
+        _lib.check(self.lib.gbn_profile(self._inner(), int(enable)), "gbn_profile")
+
+    def profile_read(self, stage: str | None = None):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        idx = -1 if stage is None else _lib.STAGES[stage]
+        _lib.check(self.lib.gbn_profile_read(self._inner(), idx, ctypes.byref(ms), ctypes.byref(n)),
+                   "gbn_profile_read")
+        return ms.value, n.value
+
+    def _inner(self):
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.gbn_toep_plan(self._h, ctypes.byref(h)), "gbn_toep_plan")
+        return h
+
     def kernel(self) -> torch.Tensor:
         """The real kernel spectrum, shape ``grid`` (device, float32)."""
         out = torch.empty(self.grid, dtype=torch.float32, device=self.device)
