@@ -236,6 +236,28 @@ int gbn_toep_power_iter(gbn_toep toep, void* x, void* x_new, double* state, floa
                         float scale, gbn_stream stream);
 
 /*
+ * Stacked NUFFT z-axis passes (stacked.py:36-330, MRIStackedNUFFT: 2D
+ * trajectory repeated on the z_index planes of a 3D image, last axis
+ * Cartesian).  gbn_stack_fwd: for C coils, per coil s_c * x (SENSE: `img` is
+ * one nx x ny x nz image and `smaps` C maps; calibless: `img` holds C
+ * images, smaps null), the centred orthonormal DFT along z divided by
+ * sqrt(2) (fftshift(fft(ifftshift(.), norm="ortho")) / sqrt(2),
+ * stacked.py:178-194), and the kept planes written as C * n_index images of
+ * nx x ny (coil major) for a 2D NUFFT of C * n_index transforms.
+ * gbn_stack_adj: the adjoint (planes back into a zero stack, inverse
+ * centred DFT / sqrt(2), coil combine with conj(smaps), or one image per
+ * coil), added to `img` when `accumulate`.
+ */
+typedef struct gbn_stack_s* gbn_stack;
+int gbn_stack_create(const int64_t* shape, const int* z_index, int n_index, int device,
+                     gbn_stack* out);
+int gbn_stack_fwd(gbn_stack stack, const void* img, const void* smaps, void* out, int C,
+                  gbn_stream stream);
+int gbn_stack_adj(gbn_stack stack, const void* in, const void* smaps, void* img, int C,
+                  int accumulate, gbn_stream stream);
+int gbn_stack_destroy(gbn_stack stack);
+
+/*
  * Stage timing.  gbn_profile(plan, 1) clears the counters and records a pair
  * of CUDA events on the launch stream around every launch of a stage;
  * gbn_profile(plan, 0) stops recording.  gbn_profile_read waits for the

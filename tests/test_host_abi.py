@@ -136,3 +136,15 @@ def test_registers_in_mrinufft_when_installed(tmp_path):
                        timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "ok" in r.stdout
+
+
+def test_traj3d2stacked_matches_reference(pkg):
+    # the reference's traj3d2stacked on a stacked2traj3d trajectory
+    from pathlib import Path
+
+    from mrinufft_gb300.stacked import traj3d2stacked
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "stacked_golden.npz")
+    t2, zi = traj3d2stacked(g["traj3d__samples3d"], 10)
+    np.testing.assert_array_equal(zi, g["traj3d__z_index"])
+    np.testing.assert_allclose(t2, g["traj3d__samples2d"])

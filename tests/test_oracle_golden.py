@@ -106,3 +106,22 @@ def test_toeplitz_oracle_matches_reference(name):
     assert rel_l2(toeplitz.apply_toeplitz(x, k), g[f"{name}__gram"]) < 1e-12
     ref = NDFTOperator(s, shape, density=w)
     assert rel_l2(ref.adj(ref.op(x)), g[f"{name}__gram"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["stack_sense", "stack_calib"])
+def test_stacked_oracle_matches_reference(name):
+    # tests/golden/stacked_golden.npz: the reference's MRIStackedNUFFT on its
+    # FP64 NDFT backend
+    from pathlib import Path
+
+    from oracle import stacked
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "stacked_golden.npz")
+    shape = tuple(int(v) for v in g[f"{name}__shape"])
+    kw = dict(smaps=g[f"{name}__smaps"] if f"{name}__smaps" in g else None,
+              n_coils=int(g[f"{name}__n_coils"]), n_batchs=int(g[f"{name}__n_batchs"]))
+    s, zi = g[f"{name}__samples"], g[f"{name}__z_index"]
+    y = stacked.stacked_op(s, shape, zi, g[f"{name}__img"], **kw)
+    assert rel_l2(y, g[f"{name}__op"]) < 1e-12
+    x = stacked.stacked_adj(s, shape, zi, g[f"{name}__ksp"], **kw)
+    assert rel_l2(x, g[f"{name}__adj"]) < 1e-12
