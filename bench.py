@@ -56,11 +56,11 @@ def parse():
     p.add_argument("--rate", type=float, default=50.0, help="c5: Poisson arrival rate (req/s)")
     p.add_argument("--saturated", type=int, default=300,
                    help="c5: requests of the saturated served-vs-plain comparison")
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "gram"],
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "gram", "stacked"],
                    help="c2: 3D 16-coil SENSE (default line); c1: 2D 256^2 single-coil radial; "
                         "c3: 32 uneven 2D instances, batched graph-captured launch vs per-call "
                         "loop; c4: differentiable forward+backward; c5: served CG stream; gram: Toeplitz "
-                        "Gram operator vs op+adj")
+                        "Gram operator vs op+adj; stacked: stack-of-stars")
     return p.parse_args()
 
 
@@ -589,6 +589,68 @@ def run_gram(args):
     print(json.dumps(line), flush=True)
 
 
+def run_stacked(args):
+    """Stacked NUFFT (stack-of-stars): radial 256 x 512 in-plane trajectory on
+    all 64 planes of a 256 x 256 x 64 image, 16 coils; op + adj per step."""
+    import torch
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    __graft_entry__.build()
+    pkg = __graft_entry__.import_package()
+    from mrinufft_gb300 import workloads
+
+    shape, C = (256, 256, 64), 16
+    s2 = workloads.radial_2d(256, 512).reshape(-1, 2).astype(np.float32)
+    smaps = workloads.coil_maps(shape, C, seed=6)
+    img = workloads.phantom(shape, seed=6)
+    op = pkg.MRIStackedGB300(s2, shape, smaps=smaps, n_coils=C, z_index=None)
+    M = op.n_samples
+    x = torch.from_numpy(img).to(dev).reshape(1, *shape)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(max(args.warmup, 3)):
+        op._adj_device(op._op_device(x))
+    torch.cuda.synchronize()
+    plan2 = op.operator.plan
+    plan2.profile(True)
+    e0.record()
+    for _ in range(args.steps):
+        op._adj_device(op._op_device(x))
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    stages = {s: plan2.profile_read(s)[0] / args.steps for s in ("pad", "fft", "interp", "spread", "crop", "zero")}
+    plan2.profile(False)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import esnufft
+
+        ncores = os.cpu_count() or 1
+        e = esnufft.EsNufft(s2.astype(np.float64) * 2 * np.pi, shape[:2], dtype=np.float32, nthreads=ncores)
+        nrm = np.sqrt(np.prod(shape[:2]) * 4)
+        planes = 8
+        z = np.fft.fftshift(np.fft.fft(np.fft.ifftshift(img * smaps[0], axes=-1), axis=-1,
+                                       norm="ortho"), axes=-1) / np.sqrt(2)
+        t = time.perf_counter()
+        for k in range(planes):
+            _ = e.type1(e.type2(np.ascontiguousarray(z[..., k])) / nrm) / nrm
+        dt = time.perf_counter() - t
+        cpu = {"value": s2.shape[0] * planes / dt / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
+               "sample": f"2D op+adj of {planes} planes of 1 coil (C/OpenMP ES spreader + scipy.fft); "
+                         "z-FFT not timed"}
+    line = {
+        "metric": "stacked NUFFT op+adj Msamples*coil/s", "value": M * C / (ms / 1e3) / 1e6, "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (radial 256 x 512 on 64 planes, ellipsoid phantom, Gaussian coil maps)",
+        "config": {"workload": "stack-of-stars 256x256x64, 16 coils, 8.4M samples, op+adj",
+                   "planes_2d_per_call": C * 64, "l2": "inputs > L2 (2D fine grids 2.1 GB)"},
+        "stage_ms_per_step_2d": stages,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def c5_templates(dev):
     """Request templates of the served mix: 2D 256^2 radial 256x512 with 8, 16,
     24 or 32 coils (70 %), 2D 384^2 spiral 32x4096 with 16 coils (20 %), 3D
@@ -721,6 +783,8 @@ def main():
         run_c4(args)
     elif args.workload == "gram":
         run_gram(args)
+    elif args.workload == "stacked":
+        run_stacked(args)
     elif args.workload == "c5":
         run_c5(args)
     else:
