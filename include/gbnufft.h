@@ -258,6 +258,22 @@ int gbn_stack_adj(gbn_stack stack, const void* in, const void* smaps, void* img,
 int gbn_stack_destroy(gbn_stack stack);
 
 /*
+ * Off-resonance correction (off_resonance.py:233-338, MRIFourierCorrected):
+ * y = sum_l B_l * A(C_l x) with time interpolators B (NK x L, complex64,
+ * row-major; sample j of a shot uses row j mod NK) and spatial interpolators
+ * C_l.  The L interpolators run as L * C transforms of one gbn_op / gbn_adj
+ * call whose coil maps are the products C_l s_c; these two passes combine
+ * them:
+ *   gbn_orc_reduce: y[b][c][j] = sum_l B[j][l] yl[b][l C + c][j]
+ *   gbn_orc_expand: yl[b][l C + c][j] = conj(B[j][l]) y[b][c][j]
+ * for nb batch items, C coils and M samples (a multiple of NK).
+ */
+int gbn_orc_reduce(const void* yl, const void* B, void* y, int nb, int L, int C, int64_t M,
+                   int64_t NK, gbn_stream stream);
+int gbn_orc_expand(const void* y, const void* B, void* yl, int nb, int L, int C, int64_t M,
+                   int64_t NK, gbn_stream stream);
+
+/*
  * Stage timing.  gbn_profile(plan, 1) clears the counters and records a pair
  * of CUDA events on the launch stream around every launch of a stage;
  * gbn_profile(plan, 0) stops recording.  gbn_profile_read waits for the

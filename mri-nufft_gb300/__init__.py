@@ -10,6 +10,7 @@ in its backend table, so ``mrinufft.get_operator("gb300")`` returns it.
 from ._lib import GB300Error, library_path, load as load_library
 from .operator import HAVE_MRINUFFT, MRIGB300, power_method
 from .stacked import MRIStackedGB300
+from .offres import MRIFourierCorrectedGB300
 from .plan import NufftPlan, dotu_f64, norm2_f64
 from ._traj import proper_trajectory
 
@@ -21,6 +22,7 @@ else:
 __all__ = [
     "MRIGB300",
     "MRIStackedGB300",
+    "MRIFourierCorrectedGB300",
     "NufftPlan",
     "GB300Error",
     "get_operator",

@@ -75,6 +75,8 @@ SIGNATURES = {
     "gbn_stack_fwd": (_c_int, [_vp, _vp, _vp, _vp, _c_int, _vp]),
     "gbn_stack_adj": (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int, _vp]),
     "gbn_stack_destroy": (_c_int, [_vp]),
+    "gbn_orc_reduce": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_i64, _c_i64, _vp]),
+    "gbn_orc_expand": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_i64, _c_i64, _vp]),
     "gbn_profile": (_c_int, [_vp, _c_int]),
     "gbn_profile_read": (_c_int, [_vp, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_i64)]),
     "gbn_norm2_f64": (_c_int, [_vp, _c_i64, _vp, _vp]),

@@ -1079,6 +1079,32 @@ int gbn_scale_ratio(int64_t n, void* x, const double* num2, const double* den2, 
                                           reinterpret_cast<cudaStream_t>(stream)));
 }
 
+int gbn_orc_reduce(const void* yl, const void* B, void* y, int nb, int L, int C, int64_t M,
+                   int64_t NK, gbn_stream stream) {
+  g_err.clear();
+  if (nb < 1 || L < 1 || C < 1 || M < 0 || NK < 1 || M % NK != 0 ||
+      (M > 0 && (!yl || !B || !y))) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  return simple_status(launch_orc_reduce(static_cast<const float2*>(yl), static_cast<const float2*>(B),
+                                         static_cast<float2*>(y), nb, L, C, M, NK,
+                                         reinterpret_cast<cudaStream_t>(stream)));
+}
+
+int gbn_orc_expand(const void* y, const void* B, void* yl, int nb, int L, int C, int64_t M,
+                   int64_t NK, gbn_stream stream) {
+  g_err.clear();
+  if (nb < 1 || L < 1 || C < 1 || M < 0 || NK < 1 || M % NK != 0 ||
+      (M > 0 && (!yl || !B || !y))) {
+    g_err = "invalid argument";
+    return GBN_ERR_ARG;
+  }
+  return simple_status(launch_orc_expand(static_cast<const float2*>(y), static_cast<const float2*>(B),
+                                         static_cast<float2*>(yl), nb, L, C, M, NK,
+                                         reinterpret_cast<cudaStream_t>(stream)));
+}
+
 int gbn_norm2_f64(const void* x, int64_t n, double* out, gbn_stream stream) {
   g_err.clear();
   if ((!x && n > 0) || !out || n < 0) {

@@ -120,6 +120,62 @@ cudaError_t launch_fill_weights(const float* w, float2* out, int64_t M, cudaStre
 }
 
 // ---------------------------------------------------------------------------
+// Off-resonance interpolator passes
+// ---------------------------------------------------------------------------
+__global__ void orc_reduce_kernel(const float2* __restrict__ yl, const float2* __restrict__ Bt,
+                                  float2* __restrict__ y, int nb, int L, int C, int64_t M,
+                                  int64_t NK) {
+  const int64_t total = (int64_t)nb * C * M;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i % M;
+    const int64_t bc = i / M;
+    const int64_t b = bc / C, c = bc - b * C;
+    const float2* brow = Bt + (j % NK) * L;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int l = 0; l < L; ++l) {
+      const float2 w = brow[l];
+      const float2 v = yl[((b * L + l) * C + c) * M + j];
+      acc.x += w.x * v.x - w.y * v.y;
+      acc.y += w.x * v.y + w.y * v.x;
+    }
+    y[i] = acc;
+  }
+}
+
+__global__ void orc_expand_kernel(const float2* __restrict__ y, const float2* __restrict__ Bt,
+                                  float2* __restrict__ yl, int nb, int L, int C, int64_t M,
+                                  int64_t NK) {
+  const int64_t total = (int64_t)nb * C * M;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i % M;
+    const int64_t bc = i / M;
+    const int64_t b = bc / C, c = bc - b * C;
+    const float2* brow = Bt + (j % NK) * L;
+    const float2 v = y[i];
+    for (int l = 0; l < L; ++l) {
+      const float2 w = brow[l];  // conj(w) * v
+      yl[((b * L + l) * C + c) * M + j] = make_float2(w.x * v.x + w.y * v.y, w.x * v.y - w.y * v.x);
+    }
+  }
+}
+
+cudaError_t launch_orc_reduce(const float2* yl, const float2* Bt, float2* y, int nb, int L, int C,
+                              int64_t M, int64_t NK, cudaStream_t st) {
+  if ((int64_t)nb * C * M == 0) return cudaSuccess;
+  orc_reduce_kernel<<<grid_for((int64_t)nb * C * M), 256, 0, st>>>(yl, Bt, y, nb, L, C, M, NK);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_orc_expand(const float2* y, const float2* Bt, float2* yl, int nb, int L, int C,
+                              int64_t M, int64_t NK, cudaStream_t st) {
+  if ((int64_t)nb * C * M == 0) return cudaSuccess;
+  orc_expand_kernel<<<grid_for((int64_t)nb * C * M), 256, 0, st>>>(y, Bt, yl, nb, L, C, M, NK);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // FP64 reductions (CG dot products and residual norms)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {

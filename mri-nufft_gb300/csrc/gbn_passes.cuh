@@ -148,6 +148,13 @@ cudaError_t launch_neg_copy(const float2* in, float2* out, int64_t n, cudaStream
 // dotu(gn, g), st[4..5] = dotu(g, g), st[6] = |gn|^2; st[7] is kept
 cudaError_t launch_cg_dots(const float2* gnew, const float2* grad, int64_t n, double* st,
                            cudaStream_t s);
+// Off-resonance time interpolators (B: NK x L, row-major; sample j of a
+// shot uses row j mod NK): reduce y[b][c][j] = sum_l B[j][l] yl[b][l C + c][j];
+// expand yl[b][l C + c][j] = conj(B[j][l]) y[b][c][j].
+cudaError_t launch_orc_reduce(const float2* yl, const float2* Bt, float2* y, int nb, int L, int C,
+                              int64_t M, int64_t NK, cudaStream_t st);
+cudaError_t launch_orc_expand(const float2* y, const float2* Bt, float2* yl, int nb, int L, int C,
+                              int64_t M, int64_t NK, cudaStream_t st);
 cudaError_t launch_pad(const PadArgs& a, cudaStream_t st);
 cudaError_t launch_crop(const CropArgs& a, cudaStream_t st);
 cudaError_t launch_norm2(const float2* x, int64_t n, double* out, cudaStream_t st);

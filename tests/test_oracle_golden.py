@@ -125,3 +125,48 @@ def test_stacked_oracle_matches_reference(name):
     assert rel_l2(y, g[f"{name}__op"]) < 1e-12
     x = stacked.stacked_adj(s, shape, zi, g[f"{name}__ksp"], **kw)
     assert rel_l2(x, g[f"{name}__adj"]) < 1e-12
+
+
+ORC = ["orc_tuple", "orc_svd", "orc_mti3d"]
+
+
+def _orc_golden():
+    from pathlib import Path
+
+    return np.load(Path(__file__).resolve().parent / "golden" / "offres_golden.npz")
+
+
+@pytest.mark.parametrize("name", ORC)
+def test_offres_formula_matches_reference(name):
+    # y = sum_l B_l * A(C_l x) on the FP64 NDFT with the reference's own
+    # interpolators reproduces the reference's MRIFourierCorrected
+    g = _orc_golden()
+    shape = tuple(int(v) for v in g[f"{name}__shape"])
+    smaps = g[f"{name}__smaps"] if f"{name}__smaps" in g else None
+    C = int(g[f"{name}__n_coils"])
+    B, Cm = g[f"{name}__B"], g[f"{name}__C"]
+    NK = B.shape[0]
+    ref = NDFTOperator(g[f"{name}__samples"], shape, n_coils=C, smaps=smaps)
+    x = g[f"{name}__img"]
+    y = sum(ref.op(Cm[l] * x).reshape(1, C, -1, NK) * B[:, l] for l in range(B.shape[1]))
+    assert rel_l2(y.reshape(1, C, -1), g[f"{name}__op"]) < 1e-12
+    yk = g[f"{name}__ksp"].reshape(1, C, -1, NK)
+    a = sum(np.conj(Cm[l]) * ref.adj((yk * np.conj(B[:, l])).reshape(1, C, -1), use_density=False)
+            for l in range(B.shape[1]))
+    assert rel_l2(a, g[f"{name}__adj"]) < 1e-12
+
+
+@pytest.mark.parametrize("name,method", [("orc_svd", "svd"), ("orc_mti3d", "mti")])
+def test_offres_factorisations_match_reference(pkg, name, method):
+    from mrinufft_gb300 import offres
+
+    g = _orc_golden()
+    fm = offres.get_complex_fieldmap_rad(g[f"{name}__b0"])
+    fn = offres.FACTORISATIONS[method]
+    B, Cm, _ = fn(field_map=fm, readout_time=g[f"{name}__t"], mask=None)
+    Bg, Cg = g[f"{name}__B"], g[f"{name}__C"]
+    assert B.shape == Bg.shape and Cm.shape == Cg.shape
+    # the interpolated phase matrix B C is independent of the basis of B
+    prod = np.einsum("kl,l...->k...", B, Cm)
+    prodg = np.einsum("kl,l...->k...", Bg, Cg)
+    assert rel_l2(prod, prodg) < 1e-4
