@@ -425,13 +425,14 @@ class MRIGB300(_Base):
         return power_method(max_iter, self, x)
 
     def pinv_solver(self, kspace_data, optim="lsqr", **kwargs):
-        """Least-squares reconstruction (base.py:667-690).  ``optim="cg"``
-        runs the device CG of :mod:`mrinufft_gb300.optim`; other solvers come
-        from mri-nufft when it is installed."""
-        if optim == "cg":
-            from .optim import cg
+        """Least-squares reconstruction (base.py:667-690).  ``optim="lsqr"``
+        (the default) and ``optim="cg"`` run the device solvers of
+        :mod:`mrinufft_gb300.optim`; other solvers come from mri-nufft when
+        it is installed."""
+        if optim in ("cg", "lsqr"):
+            from . import optim as _optim
 
-            return cg(self, kspace_data, **kwargs)
+            return getattr(_optim, optim)(self, kspace_data, **kwargs)
         try:
             from mrinufft.extras import get_optimizer  # type: ignore
         except Exception as e:

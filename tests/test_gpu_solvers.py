@@ -130,3 +130,22 @@ def test_density_true_uses_pipe(gpu_pkg):
     op = gpu_pkg.MRIGB300(traj.astype(np.float32), shape, density=True)
     w = gpu_pkg.MRIGB300.pipe(traj.astype(np.float32), shape)
     np.testing.assert_allclose(op.density.cpu().numpy(), w, rtol=1e-5)
+
+
+@pytest.mark.parametrize("name", ["lsqr_sense", "lsqr_damp", "lsqr_calib"])
+def test_lsqr_matches_reference(gpu_pkg, name):
+    # tests/golden/lsqr_golden.npz: the reference's lsqr (10 iterations) on its
+    # FP64 NDFT backend; pinv_solver's default optimizer
+    from pathlib import Path
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "lsqr_golden.npz")
+    shape = tuple(int(v) for v in g[f"{name}__shape"])
+    smaps = g[f"{name}__smaps"].astype(np.complex64) if f"{name}__smaps" in g else None
+    C, B = int(g[f"{name}__n_coils"]), int(g[f"{name}__n_batchs"])
+    op = gpu_pkg.MRIGB300(g[f"{name}__samples"].astype(np.float32), shape, n_coils=C, n_batchs=B,
+                          smaps=smaps, squeeze_dims=False)
+    kw = {"damp": float(g[f"{name}__damp"]), "max_iter": 10}
+    if f"{name}__x0" in g:
+        kw["x0"] = g[f"{name}__x0"].astype(np.complex64)
+    x = op.pinv_solver(g[f"{name}__ksp"].astype(np.complex64), **kw)
+    assert rel_l2(x, g[f"{name}__x"]) < 1e-4
