@@ -181,17 +181,22 @@ class MRIGB300(_Base):
         if callable(method):
             self.smaps = method(self.samples, self.shape, density=self.density, backend=self.backend)
             return
-        try:
-            from mrinufft.extras import get_smaps  # type: ignore
-        except Exception as e:
-            raise ValueError(f"Unknown smaps method: {method}") from e
         kwargs = {}
         if isinstance(method, dict):
             kwargs = dict(method)
             method = kwargs.pop("name")
-        smaps = get_smaps(method)(self.samples, self.shape, density=self.density,
-                                  backend=self.backend, **kwargs)
-        self.smaps = smaps
+        from .smaps import METHODS
+
+        if method in METHODS:  # estimated on the device by this package
+            fn = METHODS[method]
+            kwargs.setdefault("device", self.device.index)
+        else:
+            try:
+                from mrinufft.extras import get_smaps  # type: ignore
+            except Exception as e:
+                raise ValueError(f"Unknown smaps method: {method}") from e
+            fn = get_smaps(method)
+        self.smaps = fn(self.samples, self.shape, density=self.density, backend=self.backend, **kwargs)
 
     @property
     def density(self):
