@@ -272,9 +272,10 @@ struct gbn_plan_s {
   void setup_bins() {
     free_bins();
     stream_spread = stream_fit(g) ? 1 : 0;
+    const int last = g.dim - 1;
     ngrp = g.nb[0] * g.nb[1] * g.nb[2];
-    ncol = g.nb[0] * g.nb[1];
-    nbins = stream_spread ? ncol * g.nf[2] : ngrp;
+    ncol = ngrp / g.nb[last];
+    nbins = stream_spread ? ncol * g.nf[last] : ngrp;
     const int64_t b0 = bytes;
     sb.bin_count = dev_alloc<int>(nbins, bytes, "bins");
     sb.bin_start = dev_alloc<int>(nbins, bytes, "bins");
@@ -446,9 +447,11 @@ void run_interp(gbn_plan p, const InterpArgs& a, cudaStream_t st) {
 void run_spread(gbn_plan p, const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return;
   Span span(p, GBN_STAGE_SPREAD, st);
-  ck(a.g.dim == 2        ? launch_spread2d(a, st)
-     : p->stream_spread ? launch_spread_stream3d(a, st)
-                        : launch_spread3d(a, st),
+  // 2D: the streaming spreader for several transforms per call, the
+  // warp-cooperative one (any sort order) for a single transform
+  const bool stream = p->stream_spread && (a.g.dim == 3 || a.ntr >= 2);
+  ck(stream ? (a.g.dim == 2 ? launch_spread_stream2d(a, st) : launch_spread_stream3d(a, st))
+            : (a.g.dim == 2 ? launch_spread2d(a, st) : launch_spread3d(a, st)),
      "spread kernel");
   p->launches++;
 }
@@ -610,7 +613,9 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
     g.inv_halfw = 2.0f / w;
     g.G = 1;
     g.Nimg = 1;
-    int binsz2[2] = {32, 32};
+    // 2D: 25-cell x bins (with w <= 7 the padded column is 32 rows, one
+    // warp's lanes, for the streaming spreader)
+    int binsz2[2] = {25, 32};
     int binsz3[3] = {8, 8, 8};
     // tuning overrides: GBN_BINS2="b0,b1", GBN_BINS3="b0,b1,b2", GBN_INTERP_CG=1|2|4
     if (const char* e = std::getenv(dim == 2 ? "GBN_BINS2" : "GBN_BINS3")) {
@@ -744,7 +749,8 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
     while (maxsub < target && maxsub < cap) maxsub <<= 1;
     int64_t subcap = M / maxsub + (M < p->ngrp ? M : p->ngrp) + 1;
     // spread chunks of the streaming kernel: one CTA batch at most
-    const int maxsub_s = maxsub < kStreamChunk ? maxsub : kStreamChunk;
+    const int chunk = p->g.dim == 2 ? kStreamChunk2 : kStreamChunk;
+    const int maxsub_s = maxsub < chunk ? maxsub : chunk;
     int64_t sscap = p->stream_spread ? M / maxsub_s + (M < p->ncol ? M : p->ncol) + 1 : 0;
     if (M > p->Mcap || subcap > p->subcap || sscap > p->sscap) {
       // free the previous point buffers before the new ones (bytes tally)
@@ -775,9 +781,10 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
     int totals[2] = {0, 0};
     if (p->stream_spread) {
       const Geom& g = p->g;
-      Geom gs = g;  // sort key (x bin, y bin, z cell)
-      gs.bs[2] = 1;
-      gs.nb[2] = g.nf[2];
+      const int last = g.dim - 1;
+      Geom gs = g;  // sort key: the bins of the other axes, then the last-axis cell
+      gs.bs[last] = 1;
+      gs.nb[last] = g.nf[last];
       ck(sort_points(gs, M, k, maxsub, p->sb, st, false), "sort");
       int* q = p->grp;
       GroupBuffers gi{q, q + p->ngrp, q + 2 * p->ngrp, q + 3 * p->ngrp,
@@ -785,9 +792,11 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
       q += 4 * (size_t)p->ngrp;
       GroupBuffers gc{q, q + p->ncol, q + 2 * p->ncol, q + 3 * p->ncol,
                       p->ssub, p->ssub + p->sscap, p->ssub + 2 * p->sscap};
-      ck(build_group_table(p->ngrp, g.nb[2], g.bs[2], g.nf[2], maxsub, p->sb, gi, p->sb.d_total, st),
+      ck(build_group_table(p->ngrp, g.nb[last], g.bs[last], g.nf[last], maxsub, p->sb, gi,
+                           p->sb.d_total, st),
          "interp groups");
-      ck(build_group_table(p->ncol, 1, g.nf[2], g.nf[2], maxsub_s, p->sb, gc, p->sb.d_total + 1, st),
+      ck(build_group_table(p->ncol, 1, g.nf[last], g.nf[last], maxsub_s, p->sb, gc,
+                           p->sb.d_total + 1, st),
          "spread chunks");
     } else {
       ck(sort_points(p->g, M, k, maxsub, p->sb, st, true), "sort");

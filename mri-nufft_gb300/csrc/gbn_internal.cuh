@@ -149,8 +149,9 @@ cudaError_t launch_interp2d(const InterpArgs& a, cudaStream_t st);
 cudaError_t launch_interp3d(const InterpArgs& a, cudaStream_t st);
 cudaError_t launch_spread2d(const SpreadArgs& a, cudaStream_t st);
 cudaError_t launch_spread3d(const SpreadArgs& a, cudaStream_t st);
-// 3D column-streaming spreader; a.s is the column-chunk table
+// column-streaming spreaders; a.s is the column-chunk table
 cudaError_t launch_spread_stream3d(const SpreadArgs& a, cudaStream_t st);
+cudaError_t launch_spread_stream2d(const SpreadArgs& a, cudaStream_t st);
 cudaError_t launch_grad2d(const GradArgs& a, cudaStream_t st);
 cudaError_t launch_grad3d(const GradArgs& a, cudaStream_t st);
 
@@ -172,15 +173,19 @@ inline bool rows_fit(const Geom& g) {
   return g.dim == 3 && g.w <= 8 && g.pd[0] <= 16 && g.pd[1] <= 16 && g.pd[2] <= 16;
 }
 
-// 3D widths up to 7 with tile cross-sections up to 16 x 16 rows (and a z
-// extent that fits the kernel's 16-bit sample header) use the
-// column-streaming spreader (an 8-cell register window along z).
+// Widths up to 7 with column cross-sections of at most 16 x 16 rows (3D) or
+// 32 rows (2D), and a last-axis extent that fits the kernels' 14-bit sample
+// header, use the column-streaming spreaders (an 8-cell register window
+// along the last axis).
 inline bool stream_fit(const Geom& g) {
-  return g.dim == 3 && g.w <= 7 && g.bs[0] <= 15 && g.bs[1] <= 15 && g.pd[0] <= 16 &&
-         g.pd[1] <= 16 && g.nf[2] <= 32768 && (g.method_spread == 0 || g.method_spread == 3);
+  if (g.w > 7 || !(g.method_spread == 0 || g.method_spread == 3)) return false;
+  if (g.dim == 2) return g.pd[0] <= 32 && g.nf[1] <= 16000;
+  return g.dim == 3 && g.bs[0] <= 15 && g.bs[1] <= 15 && g.pd[0] <= 16 && g.pd[1] <= 16 &&
+         g.nf[2] <= 16000;
 }
 
-// Samples per chunk of the column-streaming spreader.
+// Samples per chunk of the column-streaming spreaders (3D, 2D).
 constexpr int kStreamChunk = 512;
+constexpr int kStreamChunk2 = 256;
 
 }  // namespace gbn

@@ -1099,6 +1099,162 @@ spread_stream3d_kernel(SpreadArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Spreading, 2D column-streaming kernel (widths w <= 7).
+//
+// The sort is keyed on (x bin, y cell) with bs0 + w <= 32, so the samples of
+// one column (bs0 cells along x, the whole y extent) arrive in y order.  A
+// CTA takes a chunk of <= kStream2Batch consecutive samples of one column;
+// lane l of every warp owns row i0 = l of the column's padded cross-section
+// (32 rows along x) and keeps an 8-cell window along y in registers (cell y
+// in slot y & 7), for the CG transforms of its warp; the CTA's warps cover
+// different transforms of the same staged samples.  Samples in y cell f
+// cover cells [f - w/2, f - w/2 + 7]; when the anchor moves, the slots that
+// leave the window are added to the fine grid with float2 atomics.  The
+// kernel weights are evaluated once per chunk for every transform.
+// ---------------------------------------------------------------------------
+constexpr int kStream2Batch = kStreamChunk2;
+
+// dynamic shared memory of the 2D streaming kernel for `coils` transforms per pass
+__host__ __device__ constexpr size_t stream2_smem_bytes(int coils) {
+  return (size_t)kStream2Batch * (sizeof(unsigned) + 16 * sizeof(float)) +
+         (size_t)coils * kStream2Batch * sizeof(float2);
+}
+
+template <int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS, 2)
+spread_stream2d_kernel(SpreadArgs a) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  const int nw = blockDim.x >> 5;
+  float* s_w1 = reinterpret_cast<float*>(s_raw);        // [batch][8], slot order (y)
+  float* s_w0 = s_w1 + kStream2Batch * 8;                // [batch][8] (x)
+  float2* s_c = reinterpret_cast<float2*>(s_w0 + kStream2Batch * 8);  // [nw * CG][batch]
+  // per sample: window anchor + 8 (bits 0-13), local row offset a0 (bits 14-19)
+  unsigned* s_hd = reinterpret_cast<unsigned*>(s_c + nw * CG * kStream2Batch);
+
+  const Geom& g = a.g;
+  const int sub = blockIdx.x;
+  const int col = a.s.sub_bin[sub];
+  const int p0 = a.s.sub_start[sub];
+  const int cnt = imin(a.s.sub_count[sub], kStream2Batch);
+  const int w = W > 0 ? W : g.w;
+  const int hw = w >> 1;
+  const int o0 = col * g.bs[0] - hw;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool own = lane < g.pd[0];
+  const int nf1 = g.nf[1];
+  const int G = (int)g.G;  // fine grids hold < 2^31 cells
+  const int rowbase = own ? wrap_idx(o0 + lane, g.nf[0]) * nf1 : 0;
+
+  // geometry of the chunk, once for every transform
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int pos = p0 + t;
+    float wt[WidthTraits<W>::WM];
+    const int a0 = weights_rt<W>(a.s.u[0][pos], g, wt) - o0;  // 0 .. bs0
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s_w0[t * 8 + k] = k < w ? wt[k] : 0.f;
+    const float u1 = a.s.u[1][pos];
+    const int zs = cell_of(u1, nf1) - hw;
+    const int off = weights_rt<W>(u1, g, wt) - zs;  // 0 or 1
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int m = k - off;
+      float v = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < WidthTraits<W>::WM; ++kk)
+        if (kk == m && kk < w) v = wt[kk];
+      s_w1[t * 8 + ((zs + k) & 7)] = v;
+    }
+    s_hd[t] = (unsigned)(zs + 8) | ((unsigned)a0 << 14);
+  }
+
+  // blockIdx.y selects the group of nw * CG transforms (one pass)
+  const int per_pass = nw * CG;
+  for (int cp = blockIdx.y * per_pass; cp < a.ntr && cp < (int)(blockIdx.y + 1) * per_pass;
+       cp += per_pass) {
+    __syncthreads();  // geometry staged
+    for (int i = threadIdx.x; i < per_pass * cnt; i += blockDim.x) {
+      const int k = i / cnt, t = i - k * cnt;
+      const int c = cp + k;
+      float2 v = make_float2(0.f, 0.f);
+      if (c < a.ntr) {
+        const int j = a.s.perm[p0 + t];
+        float dj = a.scale;
+        if (a.density) dj *= a.density[j];
+        const float2 x = a.in[(int64_t)c * a.s.M + j];
+        v = make_float2(x.x * dj, x.y * dj);
+      }
+      s_c[k * kStream2Batch + t] = v;
+    }
+    __syncthreads();
+    const int c0 = cp + warp * CG;
+    const int nc = imin(CG, a.ntr - c0);
+    if (nc <= 0 || cnt == 0) continue;
+    float ar[CG][8], ai[CG][8];
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+    float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
+    const float2* sc = s_c + warp * CG * kStream2Batch;
+    int zb = (int)(s_hd[0] & 0x3fffu) - 8;
+#pragma unroll 1
+    for (int s = 0; s < cnt; ++s) {
+      const unsigned hd = s_hd[s];
+      const int zs = (int)(hd & 0x3fffu) - 8;
+      if (zs != zb) {  // the same for every lane: flush the cells that leave the window
+        const int steps = imin(zs - zb, 8);
+        const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
+        stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+        zb = zs;
+      }
+      const unsigned r0 = (unsigned)(lane - (int)((hd >> 14) & 63u));
+      if (own && r0 < (unsigned)w) {
+        const float kw = s_w0[s * 8 + r0];
+        const float4* w4 = reinterpret_cast<const float4*>(s_w1 + s * 8);
+        const float4 wa = w4[0], wb = w4[1];
+        const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+        for (int cc = 0; cc < CG; ++cc) {
+          const float2 c = sc[cc * kStream2Batch + s];
+          const float vr = kw * c.x, vi = kw * c.y;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
+            ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
+          }
+        }
+      }
+    }
+    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+  }
+}
+
+template <int W, int CG>
+cudaError_t launch_spread_stream2d_t(const SpreadArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return cudaSuccess;
+  int nw = (a.ntr + CG - 1) / CG;
+  if (nw > GBN_THREADS / 32) nw = GBN_THREADS / 32;
+  const int passes = (a.ntr + nw * CG - 1) / (nw * CG);
+  if (passes > 65535) return cudaErrorInvalidValue;
+  const size_t smem = stream2_smem_bytes(nw * CG);
+  auto k = spread_stream2d_kernel<W, CG>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<dim3(a.s.nsub, passes), nw * 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// a.s is the column-chunk table (sub_bin = x-bin index)
+// two transforms per warp (four spill registers: measured 11 % slower on the
+// 1024-transform stack-of-stars spread)
+inline cudaError_t dispatch_spread_stream2d(const SpreadArgs& a, cudaStream_t st) {
+  const int cg = (a.ntr >= 2 && a.g.spread_cg != 1) ? 2 : 1;
+  if (a.g.w == 7)
+    return cg == 2 ? launch_spread_stream2d_t<7, 2>(a, st) : launch_spread_stream2d_t<7, 1>(a, st);
+  return cg == 2 ? launch_spread_stream2d_t<0, 2>(a, st) : launch_spread_stream2d_t<0, 1>(a, st);
+}
+
+// ---------------------------------------------------------------------------
 // Spreading, sample-driven kernel with global vector atomics (2D, and any
 // width the row kernel does not cover).  Threads take consecutive sorted
 // samples, so the float2 reductions of a warp land on nearby cells of the
