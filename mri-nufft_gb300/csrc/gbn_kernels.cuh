@@ -14,6 +14,8 @@
 //           halo cells receive contributions from several CTAs).
 #pragma once
 
+#include <cstdlib>
+
 #include "gbn_internal.cuh"
 
 // Full unrolling for compile-time widths only; the runtime-width fallback
@@ -1040,8 +1042,11 @@ spread_stream3d_kernel(SpreadArgs a) {
   }
 
   const unsigned mybit = 1u << (24 + warp);
-  for (int c0 = 0; c0 < a.ntr; c0 += CG) {
-    const int nc = imin(CG, a.ntr - c0);
+  // blockIdx.y selects a group of gridDim.y-way split transform passes
+  const int per_cta = ((a.ntr + CG - 1) / CG + gridDim.y - 1) / gridDim.y * CG;
+  const int c_end = imin(a.ntr, (int)(blockIdx.y + 1) * per_cta);
+  for (int c0 = blockIdx.y * per_cta; c0 < c_end; c0 += CG) {
+    const int nc = imin(CG, c_end - c0);
     // strengths of this pass's coils
     for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
       const int j = a.s.perm[p0 + t];
@@ -1490,7 +1495,14 @@ cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
   auto k = spread_stream3d_kernel<W, CG>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<a.s.nsub, GBN_THREADS, smem, st>>>(a);
+  // transform passes per CTA: all (1 group) unless GBN_STREAM_SPLIT asks for more groups
+  static const int split = [] {
+    const char* v = std::getenv("GBN_STREAM_SPLIT");
+    const int n = v ? std::atoi(v) : 1;
+    return n >= 1 && n <= 64 ? n : 1;
+  }();
+  const int groups = imin(split, (a.ntr + CG - 1) / CG);
+  k<<<dim3(a.s.nsub, groups), GBN_THREADS, smem, st>>>(a);
   return cudaGetLastError();
 }
 
