@@ -1,12 +1,21 @@
-"""Batched form: many uneven NUFFT instances in persistent launches.
+"""Batched form: many uneven NUFFT instances per launch sequence.
 
 ``BatchedNufft`` holds independent SENSE (or calibrationless) problems of
-different image sizes, sample counts and coil counts.  One op or adj of the
-whole batch is one persistent launch per stage of ``libgbnufft.so``
-(``gbn_batch_op`` / ``gbn_batch_adj``: pad, interp; zero, spread, crop)
-driven by per-instance work tables, plus one cuFFT call per instance; the
-op + adj step can be captured once in a CUDA graph and replayed.  Bin sizes
-and the interpolation method of every instance come from ``autotune``.
+different image sizes, sample counts and coil counts, in one of two modes:
+
+* ``"streams"`` (default): every instance keeps its own plan and runs the
+  plain backend's kernels (streaming spreaders, tile / warp interpolation,
+  pruned FFTs); the instances are spread over ``n_streams`` CUDA streams by
+  a longest-first greedy split of their work, so that small instances
+  overlap on the GPU, and the whole op + adj step is captured in one CUDA
+  graph (fork / join by events) and replayed;
+* ``"persistent"``: one persistent launch per stage of ``libgbnufft.so``
+  (``gbn_batch_op`` / ``gbn_batch_adj``: pad, interp; zero, spread, crop)
+  driven by per-instance work tables, plus one cuFFT call per fine-grid
+  size group; also capturable in a CUDA graph.
+
+Bin sizes and the interpolation method of every instance come from
+``autotune``.
 
 The reference has no such form: its only batching is ``n_trans`` chunks of
 one trajectory (``operators/base.py:904-914``, ``cufinufft.py:259-269``); the
@@ -34,9 +43,13 @@ class BatchedNufft:
         (calibrationless when no maps) and ``density`` ((M,)).
     """
 
-    def __init__(self, instances, eps=1e-6, device=None, autotune=True, tuner=None):
+    def __init__(self, instances, eps=1e-6, device=None, autotune=True, tuner=None,
+                 mode="streams", n_streams=4):
+        if mode not in ("streams", "persistent"):
+            raise ValueError("mode must be 'streams' or 'persistent'")
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.eps = eps
+        self.mode = mode
         self.plans, self.imgs, self.ksps, self.smaps, self.dens = [], [], [], [], []
         self.shapes, self.coils, self.sense, self.scales = [], [], [], []
         # the batched kernels are the dimension's defaults: tune bins and subproblem size
@@ -69,12 +82,28 @@ class BatchedNufft:
         if len(dims) != 1:
             raise ValueError("all instances of a batch must share the dimension")
         self.lib = _lib.load()
-        n = len(self.plans)
-        arr = (ctypes.c_void_p * n)(*[p._h.value for p in self.plans])
         self._h = ctypes.c_void_p()
-        _lib.check(self.lib.gbn_batch_create(n, arr, ctypes.byref(self._h)), "gbn_batch_create")
-        self._bind()
         self.graph = None
+        if mode == "persistent":
+            n = len(self.plans)
+            arr = (ctypes.c_void_p * n)(*[p._h.value for p in self.plans])
+            _lib.check(self.lib.gbn_batch_create(n, arr, ctypes.byref(self._h)), "gbn_batch_create")
+            self._bind()
+            return
+        # longest-first greedy split of the instances over the streams, by
+        # work ~ samples x coils + fine cells x coils
+        work = []
+        for plan, C, ksp in zip(self.plans, self.coils, self.ksps):
+            nf = plan.info()["nf"]
+            work.append(ksp.numel() + C * int(np.prod(nf)))
+        n_streams = max(1, min(int(n_streams), len(self.plans)))
+        loads = [0] * n_streams
+        self.groups = [[] for _ in range(n_streams)]
+        for i in sorted(range(len(work)), key=lambda i: -work[i]):
+            k = int(np.argmin(loads))
+            self.groups[k].append(i)
+            loads[k] += work[i]
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
 
     def _bind(self):
         n = len(self.plans)
@@ -113,20 +142,55 @@ class BatchedNufft:
         for buf, y in zip(self.ksps, kspaces):
             buf.copy_(_array.to_tensor(y, self.device, torch.complex64).reshape(buf.shape))
 
+    def _op_one(self, i):
+        C = self.coils[i]
+        x = self.imgs[i]
+        self.plans[i].op(x, self.smaps[i], self.ksps[i], 1, C, self.scales[i])
+
+    def _adj_one(self, i):
+        C = self.coils[i]
+        self.plans[i].adj(self.ksps[i], self.dens[i], self.smaps[i], self.imgs[i], 1, C, self.scales[i])
+
+    def _fork(self, fn):
+        """Run fn(i) for every instance on its stream, joined to the current one."""
+        cur = torch.cuda.current_stream(self.device)
+        start = torch.cuda.Event()
+        start.record(cur)
+        ends = []
+        for st, grp in zip(self.streams, self.groups):
+            st.wait_event(start)
+            with torch.cuda.stream(st):
+                for i in grp:
+                    fn(i)
+            e = torch.cuda.Event()
+            e.record(st)
+            ends.append(e)
+        for e in ends:
+            cur.wait_event(e)
+
     def op(self):
         """k-space of every instance from its bound image (in ``self.ksps``)."""
-        _lib.check(self.lib.gbn_batch_op(self._h, self.stream), "gbn_batch_op")
+        if self.mode == "persistent":
+            _lib.check(self.lib.gbn_batch_op(self._h, self.stream), "gbn_batch_op")
+        else:
+            self._fork(self._op_one)
         return self.ksps
 
     def adj(self):
         """Adjoint of every instance's bound k-space (into ``self.imgs``)."""
-        _lib.check(self.lib.gbn_batch_adj(self._h, self.stream), "gbn_batch_adj")
+        if self.mode == "persistent":
+            _lib.check(self.lib.gbn_batch_adj(self._h, self.stream), "gbn_batch_adj")
+        else:
+            self._fork(self._adj_one)
         return self.imgs
 
     def step(self):
         """op then adj of every instance (the batched benchmark step)."""
-        self.op()
-        self.adj()
+        if self.mode == "persistent":
+            self.op()
+            self.adj()
+        else:
+            self._fork(lambda i: (self._op_one(i), self._adj_one(i)))
 
     def capture(self):
         """Capture ``step`` in a CUDA graph; ``replay()`` then runs it."""

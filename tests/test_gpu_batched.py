@@ -1,4 +1,5 @@
-"""Batched form: persistent multi-instance launches == per-instance operators.
+"""Batched form (multi-stream graph and persistent work-table modes) ==
+per-instance operators.
 
 Tolerance: relative l2 <= 1e-5 between the batched and the single-instance
 results (same kernels and arithmetic, different launch decomposition), and
@@ -38,15 +39,16 @@ def _instances(rng, dim=2):
     return out
 
 
+@pytest.mark.parametrize("mode", ["streams", "persistent"])
 @pytest.mark.parametrize("dim", [2, 3])
-def test_batched_equals_single(gpu_pkg, tmp_path, dim):
+def test_batched_equals_single(gpu_pkg, tmp_path, dim, mode):
     from mrinufft_gb300.autotune import Autotuner
     from mrinufft_gb300.batched import BatchedNufft
 
     rng = np.random.default_rng(dim)
     insts = _instances(rng, dim)
     tuner = Autotuner(cache_path=tmp_path / "tune.json", interp_methods=("auto",))
-    bat = BatchedNufft(insts, tuner=tuner)
+    bat = BatchedNufft(insts, tuner=tuner, mode=mode)
     assert (tmp_path / "tune.json").exists()
     imgs = [(rng.standard_normal(i["shape"]) + 1j * rng.standard_normal(i["shape"])).astype(np.complex64)
             for i in insts]
@@ -62,13 +64,15 @@ def test_batched_equals_single(gpu_pkg, tmp_path, dim):
         assert rel_l2(x.cpu().numpy(), x_ref.cpu().numpy()) < 1e-5
 
 
-def test_batched_graph_replay(gpu_pkg, tmp_path):
+@pytest.mark.parametrize("mode", ["streams", "persistent"])
+def test_batched_graph_replay(gpu_pkg, tmp_path, mode):
     from mrinufft_gb300.autotune import Autotuner
     from mrinufft_gb300.batched import BatchedNufft
 
     rng = np.random.default_rng(11)
     insts = _instances(rng, 2)
-    bat = BatchedNufft(insts, tuner=Autotuner(cache_path=tmp_path / "t.json", interp_methods=("auto",)))
+    bat = BatchedNufft(insts, tuner=Autotuner(cache_path=tmp_path / "t.json", interp_methods=("auto",)),
+                       mode=mode)
     imgs = [(rng.standard_normal(i["shape"]) + 1j * rng.standard_normal(i["shape"])).astype(np.complex64)
             for i in insts]
     bat.set_images(imgs)
