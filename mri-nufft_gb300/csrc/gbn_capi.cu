@@ -747,7 +747,17 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
     }
     int maxsub = 32;
     while (maxsub < target && maxsub < cap) maxsub <<= 1;
-    int64_t subcap = M / maxsub + (M < p->ngrp ? M : p->ngrp) + 1;
+    // interp / grad subproblems are cut finer than the spread chunks: at most
+    // one sample per thread of the 128-thread tile interp (its weights then
+    // stay in registers across coils; measured 2.5 % faster in 3D than 512)
+    const int maxsub_i = [&] {
+      if (!p->stream_spread) return maxsub;
+      const char* e = std::getenv("GBN_INTERP_MAXSUB");
+      int v = e ? std::atoi(e) : 128;
+      if (v < 32) v = 128;
+      return v < maxsub ? v : maxsub;
+    }();
+    int64_t subcap = M / maxsub_i + (M < p->ngrp ? M : p->ngrp) + 1;
     // spread chunks of the streaming kernel: one CTA batch at most
     const int chunk = p->g.dim == 2 ? kStreamChunk2 : kStreamChunk;
     const int maxsub_s = maxsub < chunk ? maxsub : chunk;
@@ -776,7 +786,7 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
       p->sscap = sscap2;
     }
     const float* k[3] = {k0, k1, k2};
-    p->maxsub = maxsub;
+    p->maxsub = maxsub_i;
     p->maxsub_s = maxsub_s;
     int totals[2] = {0, 0};
     if (p->stream_spread) {
@@ -792,7 +802,7 @@ int gbn_setpts(gbn_plan p, int64_t M, const float* k0, const float* k1, const fl
       q += 4 * (size_t)p->ngrp;
       GroupBuffers gc{q, q + p->ncol, q + 2 * p->ncol, q + 3 * p->ncol,
                       p->ssub, p->ssub + p->sscap, p->ssub + 2 * p->sscap};
-      ck(build_group_table(p->ngrp, g.nb[last], g.bs[last], g.nf[last], maxsub, p->sb, gi,
+      ck(build_group_table(p->ngrp, g.nb[last], g.bs[last], g.nf[last], maxsub_i, p->sb, gi,
                            p->sb.d_total, st),
          "interp groups");
       ck(build_group_table(p->ncol, 1, g.nf[last], g.nf[last], maxsub_s, p->sb, gc,
