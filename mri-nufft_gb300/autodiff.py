@@ -14,21 +14,45 @@ Restates ``src/mrinufft/operators/autodiff.py:14-456`` (``_NUFFT_OP``,
   kernel-derivative interpolation of a single oversampled grid
   (``gbn_grad_traj_op`` / ``gbn_grad_traj_adj``): every axis at once, no
   extra FFT per axis.  As in the reference, density compensation does not
-  enter the backward passes.
+  enter the backward passes;
+* gradient with respect to the complex field map of an off-resonance
+  corrected operator (autodiff.py:44-56, 89-100): ``conj(x) E^H(t dy)`` for
+  the forward operator and ``conj(dx) E^H(t y)`` for the adjoint, E^H being
+  the corrected adjoint and t the readout time of every sample.  The
+  reference's forward formula multiplies by ``x`` where the derivative has
+  ``conj(x)``; this module follows the derivative.  Trajectory gradients of
+  a corrected operator run the same kernel-derivative interpolation over its
+  ``L * C`` effective coil maps.
 """
 
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import _array
+from .offres import MRIFourierCorrectedGB300
 
 
 def _dev(t, op):
     return _array.to_tensor(t, op.device, torch.complex64)
 
 
+def _meta(t):
+    return (t.device, t.dtype) if isinstance(t, torch.Tensor) else None
+
+
+def _cast(g, meta):
+    return g if meta is None else g.to(device=meta[0], dtype=meta[1])
+
+
+def _wants_field_map(op):
+    return getattr(op, "_grad_wrt_field_map", False) and isinstance(op, MRIFourierCorrectedGB300)
+
+
 def _grad_traj_op(op, x, dy):
+    if isinstance(op, MRIFourierCorrectedGB300):
+        return op._grad_traj(_dev(x, op), _dev(dy, op), adjoint=False)
     B, C = op.n_batchs, op.n_coils
     img = _dev(x, op).reshape((B if op.uses_sense else B * C), *op.shape)
     dyd = _dev(dy, op).reshape(B, C, op.n_samples)
@@ -38,6 +62,8 @@ def _grad_traj_op(op, x, dy):
 
 
 def _grad_traj_adj(op, y, dx):
+    if isinstance(op, MRIFourierCorrectedGB300):
+        return op._grad_traj(_dev(dx, op), _dev(y, op), adjoint=True)
     B, C = op.n_batchs, op.n_coils
     dxd = _dev(dx, op).reshape((B if op.uses_sense else B * C), *op.shape)
     yd = _dev(y, op).reshape(B, C, op.n_samples)
@@ -53,7 +79,7 @@ class _NUFFT_OP(torch.autograd.Function):
     def forward(ctx, x, traj, field_map, nufft_op):
         ctx.save_for_backward(x)
         ctx.nufft = nufft_op
-        ctx.traj_meta = (traj.device, traj.dtype) if isinstance(traj, torch.Tensor) else None
+        ctx.traj_meta, ctx.fm_meta = _meta(traj), _meta(field_map)
         return nufft_op.op(x)
 
     @staticmethod
@@ -61,12 +87,11 @@ class _NUFFT_OP(torch.autograd.Function):
         (x,) = ctx.saved_tensors
         op = ctx.nufft
         gx = op.adj_op(dy) if op._grad_wrt_data else None
-        gt = None
-        if op._grad_wrt_traj:
-            gt = _grad_traj_op(op, x, dy)
-            if ctx.traj_meta is not None:
-                gt = gt.to(device=ctx.traj_meta[0], dtype=ctx.traj_meta[1])
-        return gx, gt, None, None
+        gt = _cast(_grad_traj_op(op, x, dy), ctx.traj_meta) if op._grad_wrt_traj else None
+        gf = None
+        if _wants_field_map(op) and ctx.fm_meta is not None:
+            gf = _cast(op._grad_field_map(_dev(x, op), _dev(dy, op), adjoint=False), ctx.fm_meta)
+        return gx, gt, gf, None
 
 
 class _NUFFT_ADJOP(torch.autograd.Function):
@@ -76,7 +101,7 @@ class _NUFFT_ADJOP(torch.autograd.Function):
     def forward(ctx, y, traj, field_map, nufft_op):
         ctx.save_for_backward(y)
         ctx.nufft = nufft_op
-        ctx.traj_meta = (traj.device, traj.dtype) if isinstance(traj, torch.Tensor) else None
+        ctx.traj_meta, ctx.fm_meta = _meta(traj), _meta(field_map)
         return nufft_op.adj_op(y)
 
     @staticmethod
@@ -86,25 +111,27 @@ class _NUFFT_ADJOP(torch.autograd.Function):
         gy = None
         if op._grad_wrt_data:
             # forward operator without density, as autodiff.py:62-66
-            dens = op._density
-            op._density = None
+            base = getattr(op, "_fourier_op", op)
+            dens = base._density
+            base._density = None
             try:
                 gy = op.op(dx)
             finally:
-                op._density = dens
-        gt = None
-        if op._grad_wrt_traj:
-            gt = _grad_traj_adj(op, y, dx)
-            if ctx.traj_meta is not None:
-                gt = gt.to(device=ctx.traj_meta[0], dtype=ctx.traj_meta[1])
-        return gy, gt, None, None
+                base._density = dens
+        gt = _cast(_grad_traj_adj(op, y, dx), ctx.traj_meta) if op._grad_wrt_traj else None
+        gf = None
+        if _wants_field_map(op) and ctx.fm_meta is not None:
+            gf = _cast(op._grad_field_map(_dev(dx, op), _dev(y, op), adjoint=True), ctx.fm_meta)
+        return gy, gt, gf, None
 
 
 class MRINufftAutoGrad(torch.nn.Module):
     """Differentiable wrapper of a gb300 operator (autodiff.py:157-456).
 
     ``op(x)`` / ``adj_op(y)`` are differentiable with respect to the data
-    (``wrt_data``) and the trajectory (``wrt_traj``, via ``self.samples``).
+    (``wrt_data``), the trajectory (``wrt_traj``, via ``self.samples``) and,
+    for an off-resonance corrected operator, the complex field map
+    (``wrt_field_map``, via ``self.field_map``).
     With ``paired_batch`` the leading axis pairs data with coil maps and / or
     trajectories, processed one pair at a time as in the reference.
     """
@@ -113,32 +140,44 @@ class MRINufftAutoGrad(torch.nn.Module):
                  paired_batch=False):
         if any((wrt_data, wrt_traj, wrt_field_map)) and nufft_op.squeeze_dims:
             raise ValueError("Squeezing dimensions is not supported for autodiff.")
-        if wrt_field_map:
-            raise ValueError("Field-map gradients need an off-resonance operator.")
         super().__init__()
         self.nufft_op = nufft_op
         nufft_op._grad_wrt_traj = wrt_traj
         nufft_op._grad_wrt_data = wrt_data
-        nufft_op._grad_wrt_field_map = False
+        nufft_op._grad_wrt_field_map = wrt_field_map
         if wrt_traj:
             nufft_op._make_plan_grad()
             self._samples_torch = nufft_op._samples_d.clone()
             self._samples_torch.requires_grad = True
+        self._field_map_torch = None
+        if wrt_field_map and self._corrected:
+            fm = nufft_op.field_map
+            self._field_map_torch = (fm.detach().clone() if isinstance(fm, torch.Tensor)
+                                     else torch.from_numpy(np.asarray(fm, dtype=np.complex64)))
+            self._field_map_torch.requires_grad = True
         self.paired_batch = paired_batch
+
+    @property
+    def _corrected(self):
+        return isinstance(self.nufft_op, MRIFourierCorrectedGB300)
+
+    def _field_map_arg(self, field_map):
+        if field_map is not None and not self._corrected:
+            raise ValueError("Underlying nufft operator does not support field map.")
+        if self._corrected and field_map is None:
+            field_map = self.field_map
+        return field_map
 
     def op(self, x, smaps=None, samples=None, field_map=None):
         if self.paired_batch:
             return self._op_batched(x, smaps, samples)
-        if field_map is not None:
-            raise ValueError("Underlying nufft operator does not support field map.")
-        return _NUFFT_OP.apply(x, self.samples, None, self.nufft_op)
+        return _NUFFT_OP.apply(x, self.samples, self._field_map_arg(field_map), self.nufft_op)
 
     def adj_op(self, kspace, smaps=None, samples=None, field_map=None):
         if self.paired_batch:
             return self._adj_op_batched(kspace, smaps, samples)
-        if field_map is not None:
-            raise ValueError("Underlying nufft operator does not support field map.")
-        return _NUFFT_ADJOP.apply(kspace, self.samples, None, self.nufft_op)
+        return _NUFFT_ADJOP.apply(kspace, self.samples, self._field_map_arg(field_map),
+                                  self.nufft_op)
 
     def _op_batched(self, imgs, smaps=None, samples=None):
         out = []
@@ -180,6 +219,26 @@ class MRINufftAutoGrad(torch.nn.Module):
     def update_samples(self, new_samples, *, unsafe=False):
         self._samples_torch = new_samples
         self.nufft_op.update_samples(new_samples.detach(), unsafe=unsafe)
+
+    @property
+    def field_map(self):
+        """The differentiable field map (autodiff.py:381-400)."""
+        if not self._corrected:
+            raise ValueError("Underlying nufft operator does not support field map.")
+        if self._field_map_torch is not None:
+            return self._field_map_torch
+        return self.nufft_op.field_map
+
+    @field_map.setter
+    def field_map(self, value):
+        self.update_field_map(value)
+
+    def update_field_map(self, new_field_map):
+        """Set a new field map and recompute the interpolators (autodiff.py:390-400)."""
+        if not self._corrected:
+            raise ValueError("Underlying nufft operator does not support field map.")
+        self._field_map_torch = new_field_map
+        self.nufft_op.update_field_map(new_field_map.detach())
 
     def __getattr__(self, name):
         try:

@@ -147,6 +147,8 @@ class MRIFourierCorrectedGB300:
             if mask is not None:
                 mask = zoom(np.asarray(mask), zoom=f, order=0)
         self._field_map, self.mask, self.readout_time = field_map, mask, readout_time
+        self.interpolator_method = interpolators
+        self._t_dev = None
         if isinstance(interpolators, tuple):
             B, C = (np.asarray(_array.to_tensor(a, torch.device("cpu"), torch.complex64))
                     for a in interpolators)
@@ -172,7 +174,6 @@ class MRIFourierCorrectedGB300:
                         fn = get_orc_factorization(interpolators)
                 else:
                     fn = interpolators
-                self.interpolator_method = fn
                 B, C, _ = fn(field_map=field_map, readout_time=t, mask=mask, **kwargs)
                 B, C = np.asarray(B), np.asarray(C)
         self.n_shots = M // B.shape[0]
@@ -180,6 +181,48 @@ class MRIFourierCorrectedGB300:
         self.B = torch.from_numpy(np.ascontiguousarray(B, dtype=np.complex64)).to(dev)
         self.C = torch.from_numpy(np.ascontiguousarray(C, dtype=np.complex64)).to(dev).reshape(-1, *op.shape)
         self._maps = None
+
+    def update_field_map(self, new_field_map):
+        """Recompute the interpolators for a new complex field map with the
+        same method, readout time and mask (off_resonance.py:199-206)."""
+        if isinstance(new_field_map, torch.Tensor):
+            new_field_map = new_field_map.detach().cpu().numpy()
+        self.compute_interpolator(self.interpolator_method, np.asarray(new_field_map),
+                                  self.readout_time, self.mask)
+
+    @property
+    def field_map(self):
+        """The complex field map (rad/s) the interpolators were computed from."""
+        return self._field_map
+
+    @field_map.setter
+    def field_map(self, new_field_map):
+        self.update_field_map(new_field_map)
+
+    @property
+    def full_readout_time(self):
+        """``repeat(readout_time, n_shots)`` as off_resonance.py:218-222."""
+        return np.repeat(np.asarray(self.readout_time), self.n_shots)
+
+    def _sample_times(self):
+        """(M,) float32 device tensor: the readout time of every sample in the
+        layout ``op`` weights by ``B`` (sample m at time index m mod NK)."""
+        if self.readout_time is None:
+            raise ValueError("the operator has no readout time")
+        if self._t_dev is None:
+            t = np.asarray(self.readout_time, dtype=np.float32).ravel()
+            self._t_dev = torch.from_numpy(np.tile(t, self.n_shots)).to(self._fourier_op.device)
+        return self._t_dev
+
+    autograd_available = True
+
+    def make_autograd(self, *, wrt_data=True, wrt_traj=False, wrt_field_map=False,
+                      paired_batch=False):
+        """Differentiable wrapper (off_resonance.py:397-444)."""
+        from .autodiff import MRINufftAutoGrad
+
+        return MRINufftAutoGrad(self, wrt_data=wrt_data, wrt_traj=wrt_traj,
+                                wrt_field_map=wrt_field_map, paired_batch=paired_batch)
 
     @property
     def n_interpolators(self):
@@ -230,6 +273,47 @@ class MRIFourierCorrectedGB300:
                           device=op.device)
         op._plan.adj(yl, op._density, maps, out, nb, L * cc, op.inv_norm_factor, isign=-op._isign)
         return out
+
+    def _grad_field_map(self, img, k, adjoint):
+        """Gradient of a real loss with respect to the complex field map.
+
+        For ``y = E(f) x`` with ``E_mn = A_mn exp(f_n t_m)`` (holomorphic in f)
+        the cotangent ``dy`` gives ``conj(x) * E^H(t dy)``; for the adjoint
+        ``x = E(f)^H y`` (anti-holomorphic in f) the cotangent ``dx`` gives
+        ``conj(dx) * E^H(t y)`` (autodiff.py:44-56, 89-100; the forward case
+        conjugates the image, which is the exact derivative).  E^H is the
+        corrected adjoint; the sum runs over batch items and, without maps,
+        coils.  ``img`` is ``x`` (forward) or ``dx`` (adjoint), ``k`` is
+        ``dy`` (forward) or ``y`` (adjoint).
+        """
+        op = self._fourier_op
+        B, C, M = op.n_batchs, op.n_coils, op.n_samples
+        k = k.reshape(B, C, M) * self._sample_times()
+        g = self._adj_device(k)
+        img = img.reshape(g.shape)
+        return (torch.conj(img) * g).sum(dim=(0, 1)).reshape(op.shape)
+
+    def _grad_traj(self, img, k, adjoint):
+        """Trajectory gradient of the corrected forward (``adjoint=False``:
+        ``img`` = x, ``k`` = dy) or adjoint (``img`` = dx, ``k`` = y)
+        operator: the plain kernel-derivative interpolation over the L * C
+        effective maps ``C_l s_c`` with ``conj(B_l) k`` as the k-space input,
+        which is the exact derivative of ``sum_l B_l A(C_l s x)`` and of its
+        adjoint."""
+        op = self._fourier_op
+        B, C, M, L = op.n_batchs, op.n_coils, op.n_samples, self.n_interpolators
+        maps = self._effective_maps()
+        sense = op._smaps is not None
+        nb, cc = (B, C) if sense else (B * C, 1)
+        img = img.reshape(nb, *op.shape)
+        kl = torch.empty((nb, L * cc, M), dtype=torch.complex64, device=op.device)
+        _lib.check(self.lib.gbn_orc_expand(_ptr(k.reshape(nb, cc, M).contiguous()), _ptr(self.B),
+                                           _ptr(kl), nb, L, cc, M, self.n_samples_per_shot,
+                                           self._st()), "gbn_orc_expand")
+        grad = torch.empty((M, len(op.shape)), dtype=torch.float32, device=op.device)
+        fn = op.plan.grad_traj_adj if adjoint else op.plan.grad_traj_op
+        fn(img.contiguous(), maps, kl, grad, nb, L * cc, op.inv_norm_factor)
+        return grad
 
     def _squeeze(self, arr):
         if self.squeeze_dims:

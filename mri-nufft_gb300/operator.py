@@ -415,6 +415,13 @@ class MRIGB300(_Base):
     def _make_plan_grad(self, **kwargs):
         """Gradient plans share the forward plan; isign is a call argument."""
 
+    def with_off_resonance_correction(self, readout_time, b0_map=None, r2star_map=None, mask=None,
+                                      interpolator="svd"):
+        """Off-resonance corrected operator around this one (base.py:385-398)."""
+        from .offres import MRIFourierCorrectedGB300
+
+        return MRIFourierCorrectedGB300(self, b0_map, readout_time, r2star_map, mask, interpolator)
+
     def make_autograd(self, *, wrt_data=True, wrt_traj=False, paired_batch=False):
         from .autodiff import MRINufftAutoGrad
 
