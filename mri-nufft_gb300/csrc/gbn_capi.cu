@@ -641,6 +641,7 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
                         : std::strcmp(e, "wc") == 0     ? 2
                         : std::strcmp(e, "stream") == 0 ? 3
                         : std::strcmp(e, "rows") == 0   ? 4
+                        : std::strcmp(e, "quad") == 0   ? 5
                                                         : 0;
     for (int d = 0; d < 3; ++d) {
       if (d < dim) {

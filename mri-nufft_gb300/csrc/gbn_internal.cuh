@@ -39,7 +39,8 @@ struct Geom {
   int interp_cg; // coils per interp tile pass (0: automatic)
   int method_interp;  // 0: tiles, 1: direct from the fine grid, 3: double-buffered tiles
   int method_spread;  // 0: automatic, 1: global atomics, 2: warp-cooperative atomics,
-                      // 3: 3D column streaming, 4: 3D bin-tile rows
+                      // 3: 3D column streaming, 4: 3D bin-tile rows,
+                      // 5: 3D quadrant streaming (8 x 8 bins)
   int interp_threads; // CTA size of the tile interp kernel (0: 128)
   int spread_cg;      // coils per pass of the streaming spreader (0: automatic)
 };
@@ -178,7 +179,8 @@ inline bool rows_fit(const Geom& g) {
 // header, use the column-streaming spreaders (an 8-cell register window
 // along the last axis).
 inline bool stream_fit(const Geom& g) {
-  if (g.w > 7 || !(g.method_spread == 0 || g.method_spread == 3)) return false;
+  if (g.w > 7 || !(g.method_spread == 0 || g.method_spread == 3 || g.method_spread == 5))
+    return false;
   if (g.dim == 2) return g.pd[0] <= 32 && g.nf[1] <= 16000;
   return g.dim == 3 && g.bs[0] <= 15 && g.bs[1] <= 15 && g.pd[0] <= 16 && g.pd[1] <= 16 &&
          g.nf[2] <= 16000;

@@ -1104,6 +1104,183 @@ spread_stream3d_kernel(SpreadArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Spreading, 3D quadrant-streaming kernel (8 x 8 bins, widths w <= 7).
+//
+// The column-streaming kernel above gives every thread of a 256-thread CTA
+// one row of the column's 15 x 15 cross-section, so a sample's 7 x 7
+// footprint keeps 49 of 256 threads busy while all 8 warps step through it.
+// Here the chunk of an 8 x 8 column is split by footprint origin into four
+// 4 x 4 quadrants, one 128-thread CTA each: the CTA keeps the
+// chunk's samples of its quadrant, in z order, and its threads own the rows
+// of the quadrant's (4 + w) x (4 + w) cross-section (121 rows for w = 7), so
+// a sample occupies about 3 of the 4 warps.  Quadrant cross-sections overlap
+// by w rows, which the float2 flush atomics absorb.  The z window, rotated
+// weights and flush rules are those of the column kernel.
+// ---------------------------------------------------------------------------
+constexpr int kQuadThreads = 128;
+constexpr int kQuadRound = 256;  // samples staged at a time
+
+__host__ __device__ constexpr size_t quad_smem_bytes(int cg) {
+  return (size_t)kQuadRound * (sizeof(unsigned) + 24 * sizeof(float)) +
+         (size_t)cg * kQuadRound * sizeof(float2) + (size_t)kStreamBatch * sizeof(short);
+}
+
+template <int W, int CG>
+__global__ void __launch_bounds__(kQuadThreads, 4)
+spread_quad3d_kernel(SpreadArgs a) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  float* s_w2 = reinterpret_cast<float*>(s_raw);           // [kQuadRound][8], slot order
+  float* s_w0 = s_w2 + kQuadRound * 8;                      // [kQuadRound][8]
+  float* s_w1 = s_w0 + kQuadRound * 8;                      // [kQuadRound][8]
+  float2* s_c = reinterpret_cast<float2*>(s_w1 + kQuadRound * 8);  // [CG][kQuadRound]
+  // per sample: window anchor + 8 (bits 0-15), quadrant row offsets a0, a1
+  // (bits 16-19, 20-23), mask of the warps whose rows it covers (bits 24-27)
+  unsigned* s_hd = reinterpret_cast<unsigned*>(s_c + CG * kQuadRound);
+  short* s_list = reinterpret_cast<short*>(s_hd + kQuadRound);  // chunk indices, z order
+  __shared__ int s_wsum[kQuadThreads / 32];
+
+  const Geom& g = a.g;
+  // the four quadrants of a chunk are consecutive blocks, so that they run
+  // together and their overlapping rows meet in L2
+  const int sub = blockIdx.x >> 2;
+  const int col = a.s.sub_bin[sub];
+  const int p0 = a.s.sub_start[sub];
+  const int cnt = imin(a.s.sub_count[sub], kStreamBatch);
+  const int w = W > 0 ? W : g.w;
+  const int hw = w >> 1;
+  const int qx = (blockIdx.x >> 1) & 1, qy = blockIdx.x & 1;
+  const int b0 = (col / g.nb[1]) * g.bs[0] - hw;  // column origin (footprint frame)
+  const int b1 = (col % g.nb[1]) * g.bs[1] - hw;
+  const int o0 = b0 + 4 * qx, o1 = b1 + 4 * qy;   // quadrant origin
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pdq = 4 + w;
+  const int i0 = threadIdx.x / pdq, i1 = threadIdx.x - i0 * pdq;
+  const bool own = (int)threadIdx.x < pdq * pdq;
+  const int nf2 = g.nf[2];
+  const int G = (int)g.G;
+  const int rowbase = own ? (wrap_idx(o0 + i0, g.nf[0]) * g.nf[1] + wrap_idx(o1 + i1, g.nf[1])) * nf2 : 0;
+
+  // the chunk's samples whose footprint starts in this quadrant, in order
+  int n_own = 0;
+  for (int base = 0; base < cnt; base += kQuadThreads) {
+    const int t = base + threadIdx.x;
+    bool mine = false;
+    if (t < cnt) {
+      const int a0 = (int)ceilf(a.s.u[0][p0 + t] - g.halfw) - b0;  // 0 .. 8
+      const int a1 = (int)ceilf(a.s.u[1][p0 + t] - g.halfw) - b1;
+      mine = (a0 >= 4) == (qx == 1) && (a1 >= 4) == (qy == 1);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, mine);
+    if (lane == 0) s_wsum[warp] = __popc(bal);
+    __syncthreads();
+    int before = n_own, total = 0;
+#pragma unroll
+    for (int q = 0; q < kQuadThreads / 32; ++q) {
+      if (q < warp) before += s_wsum[q];
+      total += s_wsum[q];
+    }
+    if (mine) s_list[before + __popc(bal & ((1u << lane) - 1u))] = (short)t;
+    n_own += total;
+    __syncthreads();
+  }
+  if (n_own == 0) return;
+
+  auto stage_geometry = [&](int r0, int nr) {
+    for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+      const int pos = p0 + s_list[r0 + t];
+      float wt[WidthTraits<W>::WM];
+      const int a0 = weights_rt<W>(a.s.u[0][pos], g, wt) - o0;  // 0 .. 4
+#pragma unroll
+      for (int k = 0; k < 8; ++k) s_w0[t * 8 + k] = k < w ? wt[k] : 0.f;
+      const int a1 = weights_rt<W>(a.s.u[1][pos], g, wt) - o1;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) s_w1[t * 8 + k] = k < w ? wt[k] : 0.f;
+      const float u2 = a.s.u[2][pos];
+      const int zs = cell_of(u2, nf2) - hw;
+      const int off = weights_rt<W>(u2, g, wt) - zs;  // 0 or 1
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int m = k - off;
+        float v = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < WidthTraits<W>::WM; ++kk)
+          if (kk == m && kk < w) v = wt[kk];
+        s_w2[t * 8 + ((zs + k) & 7)] = v;
+      }
+      // warp q's threads own quadrant rows (32 q) / pdq .. (32 q + 31) / pdq along x
+      unsigned wm = 0;
+#pragma unroll
+      for (int q = 0; q < kQuadThreads / 32; ++q)
+        if (a0 <= imin((32 * q + 31) / pdq, pdq - 1) && a0 + w - 1 >= (32 * q) / pdq) wm |= 1u << q;
+      s_hd[t] = (unsigned)(zs + 8) | ((unsigned)a0 << 16) | ((unsigned)a1 << 20) | (wm << 24);
+    }
+  };
+  const bool once = n_own <= kQuadRound;
+  if (once) stage_geometry(0, n_own);
+
+  const unsigned mybit = 1u << (24 + warp);
+  for (int c0 = 0; c0 < a.ntr; c0 += CG) {
+    const int nc = imin(CG, a.ntr - c0);
+    float ar[CG][8], ai[CG][8];
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+    float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
+    int zb = 0;
+    for (int r0 = 0; r0 < n_own; r0 += kQuadRound) {
+      const int nr = imin(kQuadRound, n_own - r0);
+      if (!once) stage_geometry(r0, nr);
+      for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+        const int j = a.s.perm[p0 + s_list[r0 + t]];
+        float dj = a.scale;
+        if (a.density) dj *= a.density[j];
+#pragma unroll
+        for (int cc = 0; cc < CG; ++cc) {
+          float2 x = cc < nc ? a.in[(int64_t)(c0 + cc) * a.s.M + j] : make_float2(0.f, 0.f);
+          s_c[cc * kQuadRound + t] = make_float2(x.x * dj, x.y * dj);
+        }
+      }
+      __syncthreads();
+      if (r0 == 0) zb = (int)(s_hd[0] & 0xffffu) - 8;  // window: cells zb .. zb + 7
+#pragma unroll 1
+      for (int s = 0; s < nr; ++s) {
+        const unsigned hd = s_hd[s];
+        const int zs = (int)(hd & 0xffffu) - 8;
+        if (zs != zb) {  // the same for every thread: flush the cells that leave the window
+          const int steps = imin(zs - zb, 8);
+          const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
+          stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf2, G, nc);
+          zb = zs;
+        }
+        if (hd & mybit) {  // warp-uniform
+          const unsigned r0w = (unsigned)(i0 - (int)((hd >> 16) & 15u));
+          const unsigned r1w = (unsigned)(i1 - (int)((hd >> 20) & 15u));
+          if (own && r0w < (unsigned)w && r1w < (unsigned)w) {
+            const float kw = s_w0[s * 8 + r0w] * s_w1[s * 8 + r1w];
+            const float4* w4 = reinterpret_cast<const float4*>(s_w2 + s * 8);
+            const float4 wa = w4[0], wb = w4[1];
+            const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+            for (int cc = 0; cc < CG; ++cc) {
+              const float2 c = s_c[cc * kQuadRound + s];
+              const float vr = kw * c.x, vi = kw * c.y;
+#pragma unroll
+              for (int k = 0; k < 8; ++k) {
+                ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
+                ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();  // staged strengths (and geometry) are replaced next
+    }
+    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf2, G, nc);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Spreading, 2D column-streaming kernel (widths w <= 7).
 //
 // The sort is keyed on (x bin, y cell) with bs0 + w <= 32, so the samples of
@@ -1506,10 +1683,31 @@ cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+template <int W, int CG>
+cudaError_t launch_spread_quad_t(const SpreadArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return cudaSuccess;
+  const size_t smem = quad_smem_bytes(CG);
+  auto k = spread_quad3d_kernel<W, CG>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<(unsigned)(4 * (int64_t)a.s.nsub), kQuadThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 // a.s is the column-chunk table (sub_bin = column index)
 inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st) {
   int cg = a.ntr >= 3 ? 4 : a.ntr;
   if (a.g.spread_cg == 1 || a.g.spread_cg == 2 || a.g.spread_cg == 4) cg = imin(cg, a.g.spread_cg);
+  // 8 x 8 bins: quadrant CTAs (measured 7 % faster than whole columns on the
+  // 3D kooshball); GBN_SPREAD=stream keeps the column kernel
+  if ((a.g.method_spread == 0 || a.g.method_spread == 5) && a.g.bs[0] == 8 && a.g.bs[1] == 8) {
+    if (a.g.w == 7) {
+      if (cg == 4) return launch_spread_quad_t<7, 4>(a, st);
+      return cg == 2 ? launch_spread_quad_t<7, 2>(a, st) : launch_spread_quad_t<7, 1>(a, st);
+    }
+    if (cg == 4) return launch_spread_quad_t<0, 4>(a, st);
+    return cg == 2 ? launch_spread_quad_t<0, 2>(a, st) : launch_spread_quad_t<0, 1>(a, st);
+  }
   if (a.g.w == 7) {
     if (cg == 4) return launch_spread_stream_t<7, 4>(a, st);
     return cg == 2 ? launch_spread_stream_t<7, 2>(a, st) : launch_spread_stream_t<7, 1>(a, st);
