@@ -316,10 +316,9 @@ __device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) 
     // whose origins differ by a non-zero multiple of 16 cells (a float2 spans
     // two of the 32 banks) are serialised, while lanes on the same cell share
     // one broadcast.  The samples are sorted by (origin mod 16, origin) and
-    // the runs of equal origins are dealt round-robin to the half-warps that
-    // have room (runs split only when none has); in a model of the 3D
-    // kooshball this takes the wavefronts per half-warp load from 2.0 (sort
-    // order) to 1.26 (ideal 1).
+    // the runs of equal origins are dealt round-robin to the half-warps; in
+    // a model of the 3D kooshball this takes the wavefronts per half-warp
+    // load from 2.0 (sort order) to 1.29 (ideal 1).
     __shared__ int s_hist[16];
     __shared__ int s_slot[GBN_THREADS];
     __shared__ int s_key[GBN_THREADS];   // origin cell, by residue bucket
@@ -360,33 +359,63 @@ __device__ __forceinline__ void interp_body(const InterpArgs& a, const int sub) 
       s_who[sp] = threadIdx.x;
     }
     __syncthreads();
+    // Run r goes to half-warp r mod nh after the runs dealt there before it;
+    // lanes past 16 move to the free lanes of other half-warps (prefix sums
+    // of the overflow and free counts).  Everything is parallel over the
+    // CTA; in the model it keeps 98 % of the gain of a sequential deal that
+    // skips full half-warps.
+    __shared__ int s_rpos[GBN_THREADS];  // lane of run r's first sample in its half-warp
+    __shared__ int s_wcnt[GBN_THREADS / 32];
+    __shared__ int s_hfill[16], s_fpre[17], s_opre[17];
+    int* const s_rstart = s_key;  // run start positions (written after the key reads)
+    const int nh = (cnt + 15) >> 4;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int p = threadIdx.x;
+    const bool in = p < cnt;
+    const bool st = in && (p == 0 || s_key[p] != s_key[p - 1]);
+    const unsigned bal = __ballot_sync(0xffffffffu, st);
+    if (lane == 0) s_wcnt[warp] = __popc(bal);
+    __syncthreads();
+    int wpre = 0, nruns = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      if (q < warp) wpre += s_wcnt[q];
+      nruns += s_wcnt[q];
+    }
+    const int run = wpre + __popc(bal & ((2u << lane) - 1u)) - 1;  // starts at or before p
+    if (st) s_rstart[run] = p;
+    __syncthreads();
+    if ((int)threadIdx.x < nh) {
+      int acc = 0;
+      for (int rr = threadIdx.x; rr < nruns; rr += nh) {
+        s_rpos[rr] = acc;
+        acc += (rr + 1 < nruns ? s_rstart[rr + 1] : cnt) - s_rstart[rr];
+      }
+      s_hfill[threadIdx.x] = acc;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-      const int nh = (cnt + 15) >> 4;
-      int fill[GBN_THREADS / 16];
-      for (int h = 0; h < nh; ++h) fill[h] = 0;
-      int h = 0;
-      for (int p = 0; p < cnt;) {
-        const int key = s_key[p];
-        int e = p + 1;
-        while (e < cnt && s_key[e] == key) ++e;
-        const int len = e - p;
-        int pick = -1;
-        for (int d = 0; d < nh && pick < 0; ++d) {
-          const int hh = h + d < nh ? h + d : h + d - nh;
-          if (fill[hh] + len <= 16) pick = hh;
-        }
-        if (pick >= 0) {
-          for (int q = p; q < e; ++q) s_slot[pick * 16 + fill[pick]++] = s_who[q];
-          h = pick + 1 < nh ? pick + 1 : 0;
-        } else {
-          for (int q = p; q < e; ++q) {
-            int hh = 0;
-            for (int x = 1; x < nh; ++x)
-              if (fill[x] < fill[hh]) hh = x;
-            s_slot[hh * 16 + fill[hh]++] = s_who[q];
-          }
-        }
-        p = e;
+      int f = 0, ov = 0;
+      for (int h = 0; h < nh; ++h) {
+        s_fpre[h] = f;
+        s_opre[h] = ov;
+        const int fl = s_hfill[h];
+        f += fl < 16 ? 16 - fl : 0;
+        ov += fl > 16 ? fl - 16 : 0;
+      }
+      s_fpre[nh] = f;
+      s_opre[nh] = ov;
+    }
+    __syncthreads();
+    if (in) {
+      const int h = run % nh;
+      const int ln = s_rpos[run] + (p - s_rstart[run]);
+      if (ln < 16) {
+        s_slot[h * 16 + ln] = s_who[p];
+      } else {  // k-th overflow sample -> k-th free lane
+        const int k = s_opre[h] + ln - 16;
+        int hh = 0;
+        while (hh + 1 < nh && s_fpre[hh + 1] <= k) ++hh;
+        s_slot[hh * 16 + s_hfill[hh] + (k - s_fpre[hh])] = s_who[p];
       }
     }
     __syncthreads();
