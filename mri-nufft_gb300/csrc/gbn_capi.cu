@@ -613,9 +613,9 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
     g.inv_halfw = 2.0f / w;
     g.G = 1;
     g.Nimg = 1;
-    // 2D: 25-cell x bins (with w <= 7 the padded column is 32 rows, one
-    // warp's lanes, for the streaming spreader)
-    int binsz2[2] = {25, 32};
+    // 2D: 19-cell x bins (with w <= 7 the padded column is at most 26 rows,
+    // two overlapping 16-row halves of a warp in the streaming spreader)
+    int binsz2[2] = {19, 32};
     int binsz3[3] = {8, 8, 8};
     // tuning overrides: GBN_BINS2="b0,b1", GBN_BINS3="b0,b1,b2", GBN_INTERP_CG=1|2|4
     if (const char* e = std::getenv(dim == 2 ? "GBN_BINS2" : "GBN_BINS3")) {

@@ -1523,6 +1523,182 @@ spread_stream2d_kernel(SpreadArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Spreading, 2D half-warp streaming kernel (x bins of <= 19 cells, w <= 7).
+//
+// The column kernel gives lane l of a warp row l of a 32-row column, so a
+// sample's w rows keep w of 32 lanes busy.  Here the two half-warps take the
+// chunk's samples by footprint origin a0 (half 0: a0 < 17 - w, rows 0..15;
+// half 1: the rest, rows 17 - w .. 32 - w), each half in z order, and a
+// warp-iteration advances both halves by one sample: a warp updates two
+// samples per step with the same instruction stream.  Windows, rotated
+// weights, flush rules and transforms per warp are those of the column
+// kernel; the rows both halves own are flushed by both.
+// ---------------------------------------------------------------------------
+template <int W, int CG>
+__global__ void __launch_bounds__(GBN_THREADS, 2)
+spread_half2d_kernel(SpreadArgs a) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  const int nw = blockDim.x >> 5;
+  float* s_w1 = reinterpret_cast<float*>(s_raw);        // [batch][8], slot order (y)
+  float* s_w0 = s_w1 + kStream2Batch * 8;                // [batch][8] (x)
+  float2* s_c = reinterpret_cast<float2*>(s_w0 + kStream2Batch * 8);  // [nw * CG][batch]
+  // per sample: window anchor + 8 (bits 0-13), local row offset a0 (bits 14-19)
+  unsigned* s_hd = reinterpret_cast<unsigned*>(s_c + nw * CG * kStream2Batch);
+  short* s_list = reinterpret_cast<short*>(s_hd + kStream2Batch);  // [2][batch], z order
+  __shared__ int s_wsum[GBN_THREADS / 32][2];
+
+  const Geom& g = a.g;
+  const int sub = blockIdx.x;
+  const int col = a.s.sub_bin[sub];
+  const int p0 = a.s.sub_start[sub];
+  const int cnt = imin(a.s.sub_count[sub], kStream2Batch);
+  const int w = W > 0 ? W : g.w;
+  const int hw = w >> 1;
+  const int S = 17 - w;  // first footprint origin of half 1
+  const int o0 = col * g.bs[0] - hw;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int half = lane >> 4;
+  const int row = (lane & 15) + (half ? S : 0);
+  const bool own = row < g.pd[0];
+  const int nf1 = g.nf[1];
+  const int G = (int)g.G;  // fine grids hold < 2^31 cells
+  const int rowbase = own ? wrap_idx(o0 + row, g.nf[0]) * nf1 : 0;
+
+  // geometry of the chunk, once for every transform
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int pos = p0 + t;
+    float wt[WidthTraits<W>::WM];
+    const int a0 = weights_rt<W>(a.s.u[0][pos], g, wt) - o0;  // 0 .. bs0
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s_w0[t * 8 + k] = k < w ? wt[k] : 0.f;
+    const float u1 = a.s.u[1][pos];
+    const int zs = cell_of(u1, nf1) - hw;
+    const int off = weights_rt<W>(u1, g, wt) - zs;  // 0 or 1
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int m = k - off;
+      float v = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < WidthTraits<W>::WM; ++kk)
+        if (kk == m && kk < w) v = wt[kk];
+      s_w1[t * 8 + ((zs + k) & 7)] = v;
+    }
+    s_hd[t] = (unsigned)(zs + 8) | ((unsigned)a0 << 14);
+  }
+  __syncthreads();
+  // the samples of each half, in order
+  int n0 = 0, n1 = 0;
+  for (int base = 0; base < cnt; base += blockDim.x) {
+    const int t = base + threadIdx.x;
+    const bool h1 = t < cnt && (int)((s_hd[t] >> 14) & 63u) >= S;
+    const bool h0 = t < cnt && !h1;
+    const unsigned b0 = __ballot_sync(0xffffffffu, h0), b1 = __ballot_sync(0xffffffffu, h1);
+    if (lane == 0) {
+      s_wsum[warp][0] = __popc(b0);
+      s_wsum[warp][1] = __popc(b1);
+    }
+    __syncthreads();
+    int pre0 = n0, pre1 = n1, tot0 = 0, tot1 = 0;
+    for (int q = 0; q < nw; ++q) {
+      if (q < warp) {
+        pre0 += s_wsum[q][0];
+        pre1 += s_wsum[q][1];
+      }
+      tot0 += s_wsum[q][0];
+      tot1 += s_wsum[q][1];
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    if (h0) s_list[pre0 + __popc(b0 & lt)] = (short)t;
+    if (h1) s_list[kStream2Batch + pre1 + __popc(b1 & lt)] = (short)t;
+    n0 += tot0;
+    n1 += tot1;
+    __syncthreads();
+  }
+  const int nmine = half ? n1 : n0;
+  const int nmax = n0 > n1 ? n0 : n1;
+  const short* lst = s_list + (half ? kStream2Batch : 0);
+
+  // blockIdx.y selects the group of nw * CG transforms (one pass)
+  const int per_pass = nw * CG;
+  for (int cp = blockIdx.y * per_pass; cp < a.ntr && cp < (int)(blockIdx.y + 1) * per_pass;
+       cp += per_pass) {
+    __syncthreads();  // lists staged; s_c free
+    for (int i = threadIdx.x; i < per_pass * cnt; i += blockDim.x) {
+      const int k = i / cnt, t = i - k * cnt;
+      const int c = cp + k;
+      float2 v = make_float2(0.f, 0.f);
+      if (c < a.ntr) {
+        const int j = a.s.perm[p0 + t];
+        float dj = a.scale;
+        if (a.density) dj *= a.density[j];
+        const float2 x = a.in[(int64_t)c * a.s.M + j];
+        v = make_float2(x.x * dj, x.y * dj);
+      }
+      s_c[k * kStream2Batch + t] = v;
+    }
+    __syncthreads();
+    const int c0 = cp + warp * CG;
+    const int nc = imin(CG, a.ntr - c0);
+    if (nc <= 0 || cnt == 0) continue;
+    float ar[CG][8], ai[CG][8];
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+    float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
+    const float2* sc = s_c + warp * CG * kStream2Batch;
+    int zb = nmine > 0 ? (int)(s_hd[lst[0]] & 0x3fffu) - 8 : 0;
+#pragma unroll 1
+    for (int it = 0; it < nmax; ++it) {
+      if (it < nmine) {
+        const int s = lst[it];
+        const unsigned hd = s_hd[s];
+        const int zs = (int)(hd & 0x3fffu) - 8;
+        if (zs != zb) {  // the same for every lane of the half
+          const int steps = imin(zs - zb, 8);
+          const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
+          stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+          zb = zs;
+        }
+        const unsigned r0 = (unsigned)(row - (int)((hd >> 14) & 63u));
+        if (own && r0 < (unsigned)w) {
+          const float kw = s_w0[s * 8 + r0];
+          const float4* w4 = reinterpret_cast<const float4*>(s_w1 + s * 8);
+          const float4 wa = w4[0], wb = w4[1];
+          const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+          for (int cc = 0; cc < CG; ++cc) {
+            const float2 c = sc[cc * kStream2Batch + s];
+            const float vr = kw * c.x, vi = kw * c.y;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
+              ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
+            }
+          }
+        }
+      }
+    }
+    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+  }
+}
+
+template <int W, int CG>
+cudaError_t launch_spread_half2d_t(const SpreadArgs& a, cudaStream_t st) {
+  if (a.s.nsub == 0) return cudaSuccess;
+  int nw = (a.ntr + CG - 1) / CG;
+  if (nw > GBN_THREADS / 32) nw = GBN_THREADS / 32;
+  const int passes = (a.ntr + nw * CG - 1) / (nw * CG);
+  if (passes > 65535) return cudaErrorInvalidValue;
+  const size_t smem = stream2_smem_bytes(nw * CG) + 2 * kStream2Batch * sizeof(short);
+  auto k = spread_half2d_kernel<W, CG>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<dim3(a.s.nsub, passes), nw * 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 template <int W, int CG>
 cudaError_t launch_spread_stream2d_t(const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return cudaSuccess;
@@ -1543,6 +1719,12 @@ cudaError_t launch_spread_stream2d_t(const SpreadArgs& a, cudaStream_t st) {
 // 1024-transform stack-of-stars spread)
 inline cudaError_t dispatch_spread_stream2d(const SpreadArgs& a, cudaStream_t st) {
   const int cg = (a.ntr >= 2 && a.g.spread_cg != 1) ? 2 : 1;
+  // x bins of <= 19 cells: half-warp kernel unless GBN_SPREAD=stream
+  if (a.g.bs[0] <= 19 && a.g.method_spread != 3) {
+    if (a.g.w == 7)
+      return cg == 2 ? launch_spread_half2d_t<7, 2>(a, st) : launch_spread_half2d_t<7, 1>(a, st);
+    return cg == 2 ? launch_spread_half2d_t<0, 2>(a, st) : launch_spread_half2d_t<0, 1>(a, st);
+  }
   if (a.g.w == 7)
     return cg == 2 ? launch_spread_stream2d_t<7, 2>(a, st) : launch_spread_stream2d_t<7, 1>(a, st);
   return cg == 2 ? launch_spread_stream2d_t<0, 2>(a, st) : launch_spread_stream2d_t<0, 1>(a, st);
