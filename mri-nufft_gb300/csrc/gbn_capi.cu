@@ -631,6 +631,7 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
                         : std::strcmp(e, "db") == 0 ? 3
                         : std::strcmp(e, "wc") == 0 ? 4
                         : std::strcmp(e, "twc") == 0 ? 5
+                        : std::strcmp(e, "tile") == 0 ? 6
                                                      : 0;
     if (const char* e = std::getenv("GBN_INTERP_THREADS")) {
       int v = std::atoi(e);

@@ -37,7 +37,9 @@ struct Geom {
   int64_t Nimg;  // image pixels per transform
   int tile;      // padded tile cells = prod(pd)
   int interp_cg; // coils per interp tile pass (0: automatic)
-  int method_interp;  // 0: tiles, 1: direct from the fine grid, 3: double-buffered tiles
+  int method_interp;  // 0: automatic (3D tiles, 2D warp-cooperative), 1: direct from the
+                      // fine grid, 3: double-buffered tiles, 4: warp-cooperative,
+                      // 5: 3D tile warp-cooperative, 6: tiles
   int method_spread;  // 0: automatic, 1: global atomics, 2: warp-cooperative atomics,
                       // 3: 3D column streaming, 4: 3D bin-tile rows,
                       // 5: 3D quadrant streaming (8 x 8 bins)

@@ -2080,8 +2080,9 @@ inline cudaError_t launch_interp_twc(const InterpArgs& a, cudaStream_t st) {
 
 template <int DIM>
 cudaError_t dispatch_interp(const InterpArgs& a, cudaStream_t st) {
-  // 2D at w = 7 defaults to the warp-cooperative direct kernel (measured 2.7x
-  // the tile kernel on 256^2 / 384^2 multi-coil problems); 3D to tiles
+  // 2D at w = 7 defaults to the warp-cooperative direct kernel (measured 1.1x
+  // the tile kernel with its bank-aware lane order on the 1024-transform
+  // stack-of-stars, 2.7x before it); 3D to tiles.  GBN_INTERP=tile forces tiles.
   if (a.g.w == 7 && (a.g.method_interp == 4 || (DIM == 2 && a.g.method_interp == 0)))
     return launch_interp_wc_t<DIM>(a, st);
   if (DIM == 3 && a.g.method_interp == 5 && a.g.w == 7 && a.s.maxsub <= kTwcMaxSub)
