@@ -71,6 +71,24 @@ def dist_env():
     return rank, world, local
 
 
+def slowest_rank_ms(ms, world, device):
+    """The largest of every rank's time (all-reduce MAX on the default group)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
+def replica_rate(units_per_rank, world, ms):
+    """Whole-job throughput of ``world`` independent replicas, in millions of
+    units per second: every rank's units over the slowest rank's step time."""
+    return world * units_per_rank / (ms / 1e3) / 1e6
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -270,11 +288,8 @@ def run_gb300(args):
     stages = {s: plan.profile_read(s) for s in ("pad", "fft", "interp", "spread", "crop", "zero")}
     _, launches = plan.profile_read(None)
     plan.profile(False)
-    if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
-    value = world * M * C / (ms / 1e3) / 1e6
+    ms = slowest_rank_ms(ms, world, dev)
+    value = replica_rate(M * C, world, ms)
 
     # ---- end to end through the public API with pinned host buffers ----
     img_h = torch.from_numpy(img).reshape(1, *shape).pin_memory()
@@ -297,11 +312,8 @@ def run_gb300(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t)
-    e2e_value = world * M * C / (e2e_ms / 1e3) / 1e6
+    e2e_ms = slowest_rank_ms(e2e_ms, world, dev)
+    e2e_value = replica_rate(M * C, world, e2e_ms)
 
     # ---- roofline of the dominant kernel ----
     peaks_path = ROOT / "MEASURED_PEAKS.json"
