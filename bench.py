@@ -210,6 +210,46 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def accuracy_vs_ndft(op, img, traj, shape, smaps=None, coil=0, rows=None, voxels=None, seed=5):
+    """Relative l2 error of one coil's op and adj on the GPU against the FP64
+    NDFT of the oracle (the checker), on all samples / voxels or on seeded
+    subsets of them.  The adj input is that coil's op output with the other
+    coils zero, compensated by the operator's own density.  Part of the CPU
+    leg; a failure is reported in the line, not raised."""
+    try:
+        import torch
+        from oracle import ndft
+
+        shape = tuple(int(n) for n in shape)
+        ku = ndft.proper_trajectory_unit(traj)
+        M, nvox = ku.shape[0], int(np.prod(shape))
+        nrm = ndft.norm_factor(shape)
+        rng = np.random.default_rng(seed)
+        rsel = np.sort(rng.choice(M, rows, replace=False)) if rows and rows < M else np.arange(M)
+        vsel = np.sort(rng.choice(nvox, voxels, replace=False)) if voxels and voxels < nvox else np.arange(nvox)
+        sense = smaps is not None
+        x = torch.from_numpy(np.ascontiguousarray(img, dtype=np.complex64)).to(op.device)
+        y = op._op_device(x.reshape((1, *shape) if sense else (1, 1, *shape)))
+        y_c = y[0, coil].cpu().numpy()
+        xs = np.asarray(img, dtype=np.complex128) * (smaps[coil] if sense else 1)
+        y_ref = ndft.ndft_type2_rows(ku, xs, shape, rsel) / nrm
+        e_op = float(np.linalg.norm(y_c[rsel] - y_ref) / np.linalg.norm(y_ref))
+        yk = torch.zeros_like(y)
+        yk[0, coil] = y[0, coil]
+        z = op._adj_device(yk)
+        z_c = (z[0, 0] if sense else z[0, coil]).cpu().numpy().reshape(-1)
+        d = op._density
+        c = y_c.astype(np.complex128) * (1.0 if d is None else d.cpu().numpy().astype(np.float64))
+        z_ref = ndft.ndft_type1_voxels(ku, c, shape, vsel) / nrm
+        if sense:
+            z_ref = z_ref * np.conj(np.asarray(smaps[coil]).reshape(-1)[vsel])
+        e_adj = float(np.linalg.norm(z_c[vsel] - z_ref) / np.linalg.norm(z_ref))
+        return {"op_rel_l2": e_op, "adj_rel_l2": e_adj, "coil": coil, "sample_rows": int(len(rsel)),
+                "voxels": int(len(vsel)), "reference": "FP64 NDFT (oracle)"}
+    except Exception as exc:  # reported, never fatal to the bench line
+        return {"error": f"{type(exc).__name__}: {exc}"}
+
+
 def cpu_baseline(traj, shape, img, smaps, dens, n_coils):
     """Bounded sample of the CPU port: op+adj of 4 coils on all host cores."""
     from oracle import esnufft
@@ -362,6 +402,7 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(traj, shape, img, smaps,
                                             dens.cpu().numpy() if hasattr(dens, "cpu") else dens, C)
+        line["accuracy"] = accuracy_vs_ndft(op, img, traj, shape, smaps=smaps, rows=2048, voxels=64)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -482,6 +523,7 @@ def run_c1(args):
         dt = (time.perf_counter() - t) / reps
         cpu = {"value": M / dt / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": f"{reps} op+adj steps, C/OpenMP ES spreader + scipy.fft"}
+    acc = accuracy_vs_ndft(op, img, traj, shape) if not args.no_cpu_baseline else None
     line = {
         "metric": METRIC, "value": M / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1,
         "steps": steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
@@ -491,6 +533,8 @@ def run_c1(args):
                    "l2": "flushed between steps (256 MB write)"},
         "cpu_baseline": cpu,
     }
+    if acc is not None:
+        line["accuracy"] = acc
     print(json.dumps(line), flush=True)
 
 
