@@ -344,9 +344,11 @@ int gbn_scale_ratio(int64_t n, void* x, const double* num2, const double* den2, 
  * gbn_plan_create(dim, n_modes, osf, eps, 1, 1, dev) + gbn_setpts + gbn_pipe:
  * `iters` times w <- w / |scale2 * interp(spread(w))| on the n_modes grid,
  * w complex64 of length M, coordinates float32 radians, on the current
- * device.  Grids of more than GBN_STATIC_GRID_CELLS cells are rejected
- * (GBN_ERR_ARG).  The first call on a device looks the array up with
- * cudaGetSymbolAddress and should come before any stream capture.  Every
+ * device; osf <= 1 takes the osf = 2 kernel, as gbn_plan_create does.
+ * Grids of more than GBN_STATIC_GRID_CELLS cells are rejected (GBN_ERR_ARG)
+ * before anything runs.  Every call looks the array's device address up with
+ * cudaGetSymbolAddress (no allocation); the first call on a device also
+ * loads the module there and should come before any stream capture.  Every
  * call shares the array (each iteration clears it first): calls whose work
  * overlaps on the GPU race and must be serialised by the caller.
  */

@@ -81,38 +81,6 @@ void dev_free(void* p) {
   if (p) cudaFree(p);
 }
 
-// ----------------------------------------------------------------------------
-// Kernel parameters (published exponential-of-semicircle rules of the finufft
-// paper, Barnett, Magland & af Klinteberg, SISC 2019, and the finufft docs):
-//   upsampfac 2: w = ceil(-log10(eps / 10)), beta = c(w) * w with
-//                c = 2.20, 2.26, 2.38 for w = 2, 3, 4 and 2.30 otherwise;
-//   other sigma: w = ceil(-ln(eps) / (pi sqrt(1 - 1/sigma))),
-//                beta = 0.97 * pi * w * (1 - 1 / (2 sigma));
-//   w is clamped to [2, 16].
-// ----------------------------------------------------------------------------
-void kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
-  int w;
-  double beta;
-  if (sigma == 2.0) {
-    w = (int)std::ceil(-std::log10(eps / 10.0));
-  } else {
-    w = (int)std::ceil(-std::log(eps) / (M_PI * std::sqrt(1.0 - 1.0 / sigma)));
-  }
-  if (w < 2) w = 2;
-  if (w > 16) w = 16;
-  if (sigma == 2.0) {
-    double c = 2.30;
-    if (w == 2) c = 2.20;
-    else if (w == 3) c = 2.26;
-    else if (w == 4) c = 2.38;
-    beta = c * w;
-  } else {
-    beta = 0.97 * M_PI * w * (1.0 - 1.0 / (2.0 * sigma));
-  }
-  *w_out = w;
-  *beta_out = beta;
-}
-
 // smallest even integer >= n with no prime factor other than 2, 3, 5
 int64_t next_smooth_even(int64_t n) {
   if (n <= 2) return 2;

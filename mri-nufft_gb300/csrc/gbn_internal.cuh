@@ -144,6 +144,34 @@ __device__ __forceinline__ int cell_of(float u, int nf) {
   return f > nf - 1 ? nf - 1 : f;
 }
 
+// Kernel width and shape from the published exponential-of-semicircle rules
+// (finufft paper, Barnett, Magland & af Klinteberg, SISC 2019, and the finufft
+// docs); every entry point that builds a kernel takes them from here:
+//   sigma 2:     w = ceil(-log10(eps / 10)), beta = c(w) * w with
+//                c = 2.20, 2.26, 2.38 for w = 2, 3, 4 and 2.30 otherwise;
+//   other sigma: w = ceil(-ln(eps) / (pi sqrt(1 - 1/sigma))),
+//                beta = 0.97 * pi * w * (1 - 1 / (2 sigma));
+//   w is clamped to [2, 16].  A sigma <= 1 (spread-only grids whose caller
+//   gave no oversampling) takes the sigma = 2 rule.
+inline void kernel_params(double eps, double sigma, int* w_out, double* beta_out) {
+  const double pi = 3.14159265358979323846;
+  if (!(sigma > 1.0)) sigma = 2.0;
+  int w;
+  if (sigma == 2.0) w = (int)__builtin_ceil(-__builtin_log10(eps / 10.0));
+  else w = (int)__builtin_ceil(-__builtin_log(eps) / (pi * __builtin_sqrt(1.0 - 1.0 / sigma)));
+  if (w < 2) w = 2;
+  if (w > 16) w = 16;
+  double beta;
+  if (sigma == 2.0) {
+    const double c = w == 2 ? 2.20 : w == 3 ? 2.26 : w == 4 ? 2.38 : 2.30;
+    beta = c * w;
+  } else {
+    beta = 0.97 * pi * w * (1.0 - 1.0 / (2.0 * sigma));
+  }
+  *w_out = w;
+  *beta_out = beta;
+}
+
 // Sets the message returned by gbn_last_error() on the calling thread.
 void set_last_error(const char* msg);
 

@@ -12,16 +12,18 @@
 // reads it through the cache hierarchy.
 //
 // The array holds GBN_STATIC_GRID_CELLS complex64 cells (16 MiB) on every GPU
-// that loads the library, for the life of the process.  Its device address is
-// looked up with cudaGetSymbolAddress once per device, on the first call made
-// with that device current; that first call should therefore come before any
-// stream capture.  Every call shares the array, and each iteration clears it
-// before spreading; calls whose work overlaps on the GPU (other streams, other
-// threads) race on it and must be serialised by the caller.
+// that loads the library, for the life of the process.  Host code cannot use
+// the array's name as a device address, so every call looks the address up
+// with cudaGetSymbolAddress on the current device (a lookup that allocates
+// nothing and stays valid across a device reset, which a cached pointer would
+// not).  The first call on a device also loads the module there, so it should
+// come before any stream capture.  Every call shares the array, and each
+// iteration clears it before spreading; calls whose work overlaps on the GPU
+// (other streams, other threads) race on it and must be serialised by the
+// caller.
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "gbn_internal.cuh"
@@ -30,10 +32,6 @@
 namespace {
 
 static __device__ __align__(256) float2 g_static_grid[GBN_STATIC_GRID_CELLS];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_addr_mutex;
-float2* g_addr[kMaxDevices] = {nullptr};
 
 using gbn::fold_coord;
 using gbn::wrap_idx;
@@ -144,7 +142,6 @@ extern "C" int gbn_pipe_static(int dim, const int64_t* n_modes, double osf, doub
   if (dim != 2 && dim != 3) return fail_static(GBN_ERR_ARG, "dim must be 2 or 3");
   if (!n_modes) return fail_static(GBN_ERR_ARG, "null n_modes");
   if (!(eps > 0.0 && eps < 1.0)) return fail_static(GBN_ERR_ARG, "eps must be in (0, 1)");
-  if (!(osf > 1.0)) return fail_static(GBN_ERR_ARG, "osf must be > 1");
   if (M < 0 || M > ((int64_t)1 << 31) - 1) return fail_static(GBN_ERR_ARG, "M out of range");
   if (iters < 0) return fail_static(GBN_ERR_ARG, "iters must be >= 0");
   if (M > 0 && (!k0 || !k1 || (dim == 3 && !k2) || !w))
@@ -155,62 +152,46 @@ extern "C" int gbn_pipe_static(int dim, const int64_t* n_modes, double osf, doub
   for (int d = 0; d < 3; ++d) {
     if (d < dim) {
       if (n_modes[d] < 1) return fail_static(GBN_ERR_ARG, "image size must be >= 1");
-      if (n_modes[d] > GBN_STATIC_GRID_CELLS)
-        return fail_static(GBN_ERR_ARG, "image larger than the static grid");
+      // cells <= GBN_STATIC_GRID_CELLS before this factor, so the test
+      // below cannot overflow and the product stays within the array
+      if (n_modes[d] > GBN_STATIC_GRID_CELLS / cells) {
+        return fail_static(GBN_ERR_ARG,
+                           "grid exceeds the static grid of " +
+                               std::to_string((long long)GBN_STATIC_GRID_CELLS) +
+                               " cells (16 MiB); use a plan (gbn_plan_create + gbn_pipe) instead");
+      }
+      cells *= n_modes[d];
       g.nf[d] = (int)n_modes[d];
       g.uscale[d] = (float)((double)n_modes[d] / (2.0 * M_PI));
-      cells *= n_modes[d];  // each factor <= 2^21: no overflow
     } else {
       g.nf[d] = 1;
       g.uscale[d] = 0.f;
     }
   }
-  if (cells > GBN_STATIC_GRID_CELLS) {
-    return fail_static(GBN_ERR_ARG,
-                       "grid of " + std::to_string((long long)cells) + " cells exceeds the static "
-                       "grid of " + std::to_string((long long)GBN_STATIC_GRID_CELLS) +
-                       " cells (16 MiB); use a plan (gbn_plan_create + gbn_pipe) instead");
-  }
-  // kernel width and shape: the published ES rules used by gbn_plan_create
+  // kernel width and shape: the rule gbn_plan_create uses (osf <= 1 takes
+  // the osf = 2 kernel there too)
   int wd;
   double beta;
-  if (osf == 2.0) wd = (int)std::ceil(-std::log10(eps / 10.0));
-  else wd = (int)std::ceil(-std::log(eps) / (M_PI * std::sqrt(1.0 - 1.0 / osf)));
-  if (wd < 2) wd = 2;
-  if (wd > 16) wd = 16;
-  if (osf == 2.0) {
-    double c = wd == 2 ? 2.20 : wd == 3 ? 2.26 : wd == 4 ? 2.38 : 2.30;
-    beta = c * wd;
-  } else {
-    beta = 0.97 * M_PI * wd * (1.0 - 1.0 / (2.0 * osf));
-  }
+  gbn::kernel_params(eps, osf, &wd, &beta);
   g.w = wd;
   g.beta = (float)beta;
   g.halfw = 0.5f * wd;
   g.inv_halfw = 2.0f / wd;
 
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail_static(GBN_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail_static(GBN_ERR_CUDA, "device ordinal out of range");
   float2* grid = nullptr;
   {
-    std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_static_grid);
-      if (e != cudaSuccess)
-        return fail_static(GBN_ERR_CUDA,
-                           std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      g_addr[dev] = static_cast<float2*>(p);
-    }
-    grid = g_addr[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_grid);
+    if (e != cudaSuccess)
+      return fail_static(GBN_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    grid = static_cast<float2*>(p);
   }
   if (M == 0 || iters == 0) return GBN_OK;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const unsigned blocks = (unsigned)((M + 255) / 256);
   float2* wv = static_cast<float2*>(w);
   const float* kk2 = dim == 3 ? k2 : k1;
+  cudaError_t e = cudaSuccess;
   for (int it = 0; it < iters; ++it) {
     e = cudaMemsetAsync(grid, 0, sizeof(float2) * (size_t)cells, st);
     if (e != cudaSuccess) return fail_static(GBN_ERR_CUDA, std::string("clear grid: ") + cudaGetErrorString(e));

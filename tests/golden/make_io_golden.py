@@ -22,6 +22,9 @@ from pathlib import Path
 
 import numpy as np
 
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from _refsrc import reference_src  # noqa: E402
+
 
 def digest(a):
     a = np.ascontiguousarray(a)
@@ -118,4 +121,4 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    main(reference_src())

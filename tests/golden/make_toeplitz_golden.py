@@ -2,7 +2,7 @@
 
 Run in a container where the reference sources are present::
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_toeplitz_golden.py /root/reference/src
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_toeplitz_golden.py <mri-nufft src>
 
 It imports ``mrinufft`` from the given source tree and, on the reference's FP64
 NDFT backend ``MRInumpy`` (``operators/interfaces/nudft_numpy.py``, float64
@@ -20,6 +20,9 @@ import sys
 from pathlib import Path
 
 import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from _refsrc import reference_src  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 
@@ -56,4 +59,4 @@ def main(ref_src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    main(reference_src())

@@ -68,15 +68,46 @@ def test_static_pipe_matches_plan_pipe(gpu_pkg):
             assert err < TOL, (shape, err)
 
 
-def test_static_pipe_rejects_oversize_grid(gpu_pkg):
+@pytest.mark.parametrize("dims", [(256, 256, 256), (2097152, 2097152, 2097152), (1, 2097153, 1),
+                                  (2048, 1025, 1)])
+def test_static_pipe_rejects_oversize_grid(gpu_pkg, dims):
+    """Grids beyond the array, including sizes whose cell count would not fit
+    64 bits, are refused before anything runs and leave w untouched."""
     lib = gpu_pkg.load_library()
     k = torch.zeros((4, 3), dtype=torch.float32, device="cuda")
     cols = [k[:, d].contiguous() for d in range(3)]
     w = torch.ones(4, dtype=torch.complex64, device="cuda")
-    dims = (ctypes.c_int64 * 3)(256, 256, 256)
+    cdims = (ctypes.c_int64 * 3)(*dims)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    st = lib.gbn_pipe_static(3, dims, 2.0, 1e-6, 4, *[ctypes.c_void_p(c.data_ptr()) for c in cols],
+    st = lib.gbn_pipe_static(3, cdims, 2.0, 1e-6, 4, *[ctypes.c_void_p(c.data_ptr()) for c in cols],
                              ctypes.c_void_p(w.data_ptr()), 1, 1.0, stream)
+    torch.cuda.synchronize()
     assert st == 1
     assert b"exceeds the static grid" in lib.gbn_last_error()
     assert torch.all(w == 1)
+
+
+def test_static_pipe_osf_rule_matches_plan(gpu_pkg):
+    """An oversampling factor <= 1 takes the osf = 2 kernel on both paths."""
+    lib = gpu_pkg.load_library()
+    from mrinufft_gb300 import workloads
+
+    shape = (40, 40)
+    k = torch.from_numpy(workloads.radial_2d(96, 32).reshape(-1, 2).astype(np.float32) *
+                         np.float32(2 * np.pi)).cuda()
+    scale2 = 1.0 / (np.prod(shape) * 4.0)
+    plan = gpu_pkg.NufftPlan(shape, eps=1e-6, upsampfac=1.0, ntrans=1, spread_only=True)
+    plan.setpts(k)
+    ref = torch.ones(k.shape[0], dtype=torch.complex64, device="cuda")
+    plan.pipe(ref, 5, scale2)
+    cols = [k[:, d].contiguous() for d in range(2)]
+    w = torch.ones(k.shape[0], dtype=torch.complex64, device="cuda")
+    dims = (ctypes.c_int64 * 2)(*shape)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = lib.gbn_pipe_static(2, dims, 1.0, 1e-6, k.shape[0], ctypes.c_void_p(cols[0].data_ptr()),
+                             ctypes.c_void_p(cols[1].data_ptr()), None, ctypes.c_void_p(w.data_ptr()),
+                             5, scale2, stream)
+    assert st == 0, lib.gbn_last_error()
+    torch.cuda.synchronize()
+    err = float(torch.linalg.vector_norm(w - ref) / torch.linalg.vector_norm(ref))
+    assert err < TOL, err
