@@ -210,42 +210,52 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def accuracy_vs_ndft(op, img, traj, shape, smaps=None, coil=0, rows=None, voxels=None, seed=5):
-    """Relative l2 error of one coil's op and adj on the GPU against the FP64
-    NDFT of the oracle (the checker), on all samples / voxels or on seeded
-    subsets of them.  The adj input is that coil's op output with the other
-    coils zero, compensated by the operator's own density.  Part of the CPU
-    leg; a failure is reported in the line, not raised."""
+def accuracy_vs_ndft(op, img, traj, shape, smaps=None, n_coils=1, rows=None, vox_per_axis=None,
+                     seed=5):
+    """Relative l2 error of the GPU op and adj against the FP64 NDFT of the
+    oracle (the checker): op on ``rows`` seeded samples (all when None) of up
+    to 4 seeded coils; adj of those coils' op output (other coils zero,
+    compensated by the operator's own density) on a seeded product set of
+    ``vox_per_axis`` indices per axis (all voxels when None).  Part of the
+    CPU leg; a failure is reported in the line, not raised."""
     try:
         import torch
         from oracle import ndft
 
         shape = tuple(int(n) for n in shape)
-        ku = ndft.proper_trajectory_unit(traj)
-        M, nvox = ku.shape[0], int(np.prod(shape))
+        k = ndft.proper_trajectory_unit(traj)
+        M = k.shape[0]
         nrm = ndft.norm_factor(shape)
         rng = np.random.default_rng(seed)
         rsel = np.sort(rng.choice(M, rows, replace=False)) if rows and rows < M else np.arange(M)
-        vsel = np.sort(rng.choice(nvox, voxels, replace=False)) if voxels and voxels < nvox else np.arange(nvox)
         sense = smaps is not None
+        C = smaps.shape[0] if sense else n_coils
+        coils = np.sort(rng.choice(C, min(C, 4), replace=False))
         x = torch.from_numpy(np.ascontiguousarray(img, dtype=np.complex64)).to(op.device)
         y = op._op_device(x.reshape((1, *shape) if sense else (1, 1, *shape)))
-        y_c = y[0, coil].cpu().numpy()
-        xs = np.asarray(img, dtype=np.complex128) * (smaps[coil] if sense else 1)
-        y_ref = ndft.ndft_type2_rows(ku, xs, shape, rsel) / nrm
-        e_op = float(np.linalg.norm(y_c[rsel] - y_ref) / np.linalg.norm(y_ref))
+        yh = y[0].cpu().numpy()
+        xs = np.asarray(img, dtype=np.complex128)
+        e_op = []
+        for c in coils:
+            ref = ndft.ndft_type2(k[rsel], xs * (smaps[c] if sense else 1), shape) / nrm
+            e_op.append(float(np.linalg.norm(yh[c, rsel] - ref) / np.linalg.norm(ref)))
         yk = torch.zeros_like(y)
-        yk[0, coil] = y[0, coil]
-        z = op._adj_device(yk)
-        z_c = (z[0, 0] if sense else z[0, coil]).cpu().numpy().reshape(-1)
+        yk[0, coils] = y[0, coils]
+        z = op._adj_device(yk)[0].cpu().numpy()
+        idx = [np.sort(rng.choice(n, min(n, vox_per_axis or n), replace=False)) for n in shape]
+        sub = np.ix_(*idx)
         d = op._density
-        c = y_c.astype(np.complex128) * (1.0 if d is None else d.cpu().numpy().astype(np.float64))
-        z_ref = ndft.ndft_type1_voxels(ku, c, shape, vsel) / nrm
+        cin = yh[coils].astype(np.complex128) * (1.0 if d is None else d.cpu().numpy().astype(np.float64))
+        t1 = ndft.ndft_type1_grid(k, cin, shape, idx) / nrm
         if sense:
-            z_ref = z_ref * np.conj(np.asarray(smaps[coil]).reshape(-1)[vsel])
-        e_adj = float(np.linalg.norm(z_c[vsel] - z_ref) / np.linalg.norm(z_ref))
-        return {"op_rel_l2": e_op, "adj_rel_l2": e_adj, "coil": coil, "sample_rows": int(len(rsel)),
-                "voxels": int(len(vsel)), "reference": "FP64 NDFT (oracle)"}
+            ref = sum(np.conj(smaps[c][sub]) * t1[q] for q, c in enumerate(coils))
+            got = z[0][sub]
+        else:
+            ref, got = t1[0], z[coils[0]][sub]
+        e_adj = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        return {"op_rel_l2": max(e_op), "op_rel_l2_per_coil": e_op, "adj_rel_l2": e_adj,
+                "coils": [int(c) for c in coils], "sample_rows": int(len(rsel)),
+                "voxels": int(np.prod([len(i) for i in idx])), "reference": "FP64 NDFT (oracle)"}
     except Exception as exc:  # reported, never fatal to the bench line
         return {"error": f"{type(exc).__name__}: {exc}"}
 
@@ -268,6 +278,50 @@ def cpu_baseline(traj, shape, img, smaps, dens, n_coils):
                       f"({dt:.1f} s), C/OpenMP ES spreader + scipy.fft"}
 
 
+def measure_pipe(pkg, samples_d, shape, device, iters=10, reps=5):
+    """Warm timing of the pipe density estimate (10 iterations of
+    w <- w / |interp(spread(w))| on the image-size grid) on a resident
+    spread-only plan, CUDA events over ``reps`` calls after an untimed one,
+    with the per-stage times of the spread and interp kernels; and the whole
+    ``MRIGB300.pipe`` call (plan creation, sort, iterations, normalisation
+    NUFFT pair) timed warm on the host."""
+    import torch
+
+    dev = samples_d.device
+    M = samples_d.shape[0]
+    pplan = pkg.NufftPlan(shape, eps=1e-6, upsampfac=2.0, ntrans=1, spread_only=True, device=device)
+    pplan.setpts(samples_d)
+    nrm2 = float(np.prod(shape) * 2 ** len(shape))
+    w = torch.ones(M, dtype=torch.complex64, device=dev)
+    pplan.pipe(w, iters, 1.0 / nrm2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pplan.profile(True)
+    e0.record()
+    for _ in range(reps):
+        w.fill_(1.0)
+        pplan.pipe(w, iters, 1.0 / nrm2)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    st = {s_: pplan.profile_read(s_) for s_ in ("spread", "interp", "zero")}
+    pplan.profile(False)
+    info = pplan.info()
+    G_t = touched_cells(samples_d, info["nf"], info["width"])
+    spread_ms = st["spread"][0] / max(1, st["spread"][1])
+    bytes_spread = 4 * len(shape) * M + 8 * M + 8 * G_t
+    t0 = time.perf_counter()
+    pkg.MRIGB300.pipe(samples_d, shape, max_iter=iters, device=device)
+    torch.cuda.synchronize()
+    whole_ms = (time.perf_counter() - t0) * 1e3
+    return {"iterations": iters, "ms_per_call": ms, "ms_per_iteration": ms / iters,
+            "stage_ms_per_iteration": {k_: v[0] / (reps * iters) for k_, v in st.items()},
+            "grid": list(info["nf"]), "touched_cells": G_t,
+            "spread_algorithmic_bytes": bytes_spread,
+            "spread_achieved_gbs": bytes_spread / (spread_ms / 1e3) / 1e9,
+            "whole_call_warm_ms": whole_ms}
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -288,12 +342,13 @@ def run_gb300(args):
     t0 = time.perf_counter()
     dens = pkg.MRIGB300.pipe(torch.from_numpy(traj).to(dev), shape, max_iter=10, device=local)
     torch.cuda.synchronize()
-    pipe_ms = (time.perf_counter() - t0) * 1e3
+    pipe_cold_ms = (time.perf_counter() - t0) * 1e3
 
     op = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps, density=dens, squeeze_dims=False,
                       device=local)
     plan = op.plan
     img_d = torch.from_numpy(img).to(dev).reshape(1, *shape)
+    pipe = measure_pipe(pkg, op._samples_d, shape, local)
 
     def step():
         y = op._op_device(img_d)
@@ -355,6 +410,29 @@ def run_gb300(args):
     e2e_ms = slowest_rank_ms(e2e_ms, world, dev)
     e2e_value = replica_rate(M * C, world, e2e_ms)
 
+    # ---- end to end with numpy host arrays (mri-nufft's CPU-array calling
+    # convention: pageable numpy in, numpy out, every copy inside the call) ----
+    img_np = np.ascontiguousarray(img.reshape(1, *shape))
+
+    def step_np():
+        return op.adj_op(op.op(img_np))
+
+    for _ in range(max(args.warmup, 1)):
+        step_np()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    nsteps_np = max(3, args.steps // 4)
+    for _ in range(nsteps_np):
+        out_np = step_np()
+    np_ms = (time.perf_counter() - t0) * 1e3 / nsteps_np
+    np_ms = slowest_rank_ms(np_ms, world, dev)
+    e2e_np = {"value": replica_rate(M * C, world, np_ms), "unit": UNIT, "ms_per_step": np_ms,
+              "steps": nsteps_np,
+              "h2d_bytes_per_step": img_np.nbytes + M * C * 8,
+              "d2h_bytes_per_step": M * C * 8 + int(np.asarray(out_np).nbytes),
+              "call": "op.adj_op(op.op(numpy image)) -> numpy image; host-timed"}
+
     # ---- roofline of the dominant kernel ----
     peaks_path = ROOT / "MEASURED_PEAKS.json"
     if peaks_path.exists():
@@ -389,7 +467,7 @@ def run_gb300(args):
         "data": "synthetic (seeded kooshball, ellipsoid phantom, Gaussian coil maps)",
         "config": {"workload": WORKLOAD, "samples": M, "coils": C, "image": list(shape),
                    "fine_grid": list(info["nf"]), "kernel_width": info["width"], "eps": 1e-6,
-                   "touched_fine_cells": G_t, "coils_per_pass": T, "pipe_ms": pipe_ms,
+                   "touched_fine_cells": G_t, "coils_per_pass": T,
                    "l2": "inputs > L2 (fine grids 2.1 GB, k-space 268 MB)",
                    "parallelism": f"replicas x{world}"},
         "stage_ms_per_step": {s: v[0] / args.steps for s, v in stages.items()},
@@ -397,12 +475,18 @@ def run_gb300(args):
         "clocks": clocks,
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": img_h.numel() * 8, "d2h_bytes_per_step": out_h.numel() * 8},
+                "h2d_bytes_per_step": img_h.numel() * 8, "d2h_bytes_per_step": out_h.numel() * 8,
+                "call": "op.adj_op(op.op(x)) on a device copy of a pinned host image, result "
+                        "copied back to pinned host memory; CUDA events"},
+        "e2e_numpy": e2e_np,
+        "pipe": dict(pipe, cold_ms=pipe_cold_ms, peak_gbs=peak,
+                     roofline_frac=pipe["spread_achieved_gbs"] / peak),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(traj, shape, img, smaps,
                                             dens.cpu().numpy() if hasattr(dens, "cpu") else dens, C)
-        line["accuracy"] = accuracy_vs_ndft(op, img, traj, shape, smaps=smaps, rows=2048, voxels=64)
+        line["accuracy"] = accuracy_vs_ndft(op, img, traj, shape, smaps=smaps, rows=4096,
+                                            vox_per_axis=16)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -523,6 +607,18 @@ def run_c1(args):
         dt = (time.perf_counter() - t) / reps
         cpu = {"value": M / dt / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": f"{reps} op+adj steps, C/OpenMP ES spreader + scipy.fft"}
+        # the reference's own CPU accuracy oracle for this case: MRInumpy's
+        # FP64 NDFT (nudft_numpy.py:58-81), as restated by the oracle
+        from oracle import ndft
+
+        ku = ndft.proper_trajectory_unit(traj)
+        t = time.perf_counter()
+        yy = ndft.ndft_type2(ku, img, shape)
+        _ = ndft.ndft_type1(ku, yy, shape)
+        cpu["ndft_fp64"] = {"s_per_op_adj": time.perf_counter() - t,
+                            "value": M / (time.perf_counter() - t) / 1e6, "unit": UNIT,
+                            "sample": "one exact FP64 op+adj (factorised NDFT of the oracle, "
+                                      "restating MRInumpy's implicit type 1 / type 2)"}
     acc = accuracy_vs_ndft(op, img, traj, shape) if not args.no_cpu_baseline else None
     line = {
         "metric": METRIC, "value": M / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1,
@@ -791,21 +887,9 @@ def c5_templates(dev):
     pkg = __graft_entry__.import_package()
     from mrinufft_gb300 import workloads
 
-    rng = np.random.default_rng(5)
-    specs = [("a8", 0.175, "radial", (256, 256), 8), ("a16", 0.175, "radial", (256, 256), 16),
-             ("a24", 0.175, "radial", (256, 256), 24), ("a32", 0.175, "radial", (256, 256), 32),
-             ("b16", 0.2, "spiral", (384, 384), 16), ("c8", 0.1, "koosh", (128, 128, 128), 8)]
     out = []
-    for key, prob, kind, shape, C in specs:
-        if kind == "radial":
-            traj = workloads.radial_2d(256, 512).reshape(-1, 2)
-        elif kind == "spiral":
-            traj = workloads.spiral_2d(32, 4096, power=2).reshape(-1, 2)
-        else:
-            traj = workloads.kooshball_3d(2048, 512).reshape(-1, 3)
-        traj = traj.astype(np.float32)
-        smaps = workloads.coil_maps(shape, C, seed=len(out))
-        x = workloads.phantom(shape, seed=len(out))
+    for i, (key, prob, kind, shape, C) in enumerate(workloads.SERVE_MIX):
+        traj, smaps, x = workloads.serve_template(i)
         op = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps, squeeze_dims=False, device=dev.index)
         y = op.op(torch.from_numpy(x).to(dev)).reshape(C, -1)
         y = y + 0.01 * torch.randn_like(y)

@@ -1966,14 +1966,9 @@ cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
   auto k = spread_stream3d_kernel<W, CG>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  // transform passes per CTA: all (1 group) unless GBN_STREAM_SPLIT asks for more groups
-  static const int split = [] {
-    const char* v = std::getenv("GBN_STREAM_SPLIT");
-    const int n = v ? std::atoi(v) : 1;
-    return n >= 1 && n <= 64 ? n : 1;
-  }();
-  const int groups = imin(split, (a.ntr + CG - 1) / CG);
-  k<<<dim3(a.s.nsub, groups), GBN_THREADS, smem, st>>>(a);
+  // one CTA per chunk runs every transform pass (the kernel also accepts a
+  // split of the passes over blockIdx.y groups)
+  k<<<dim3(a.s.nsub, 1), GBN_THREADS, smem, st>>>(a);
   return cudaGetLastError();
 }
 

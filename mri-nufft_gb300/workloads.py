@@ -3,9 +3,9 @@
 The trajectory generators restate mri-nufft's own initialisations
 (``src/mrinufft/trajectories/inits/radial.py:12-43`` for 2D radial,
 ``inits/spiral.py:26-130`` for algebraic spirals, ``KMAX = 0.5`` of
-``trajectories/utils.py:18``), and the 3D kooshball places radial spokes
-along a Fibonacci (golden-angle) sphere lattice, the distribution of
-``initialize_3D_phyllotaxis_radial`` (radial.py:46-94).  Phantoms are sums of
+``trajectories/utils.py:18``, and ``initialize_3D_phyllotaxis_radial``,
+radial.py:46-94, for the 3D kooshball); ``tests/test_workloads.py`` checks
+them against fixtures written by those generators.  Phantoms are sums of
 random ellipses / ellipsoids with complex amplitudes plus complex Gaussian
 noise; coil maps are complex Gaussians centred on a sphere, normalised so
 that sum_c |s_c|^2 = 1 at every voxel.
@@ -48,14 +48,21 @@ def spiral_2d(Nc: int, Ns: int, power: float = 1.0, nb_revolutions: float = 1.0)
 
 
 def kooshball_3d(Nc: int, Ns: int) -> np.ndarray:
-    """(Nc, Ns, 3) centre-out spokes along a Fibonacci sphere lattice."""
-    i = np.arange(Nc) + 0.5
-    z = 1 - 2 * i / Nc
-    r = np.sqrt(1 - z * z)
+    """(Nc, Ns, 3) centre-out phyllotaxis spokes (radial.py:46-94).
+
+    The reference builds them as zero-width 3D cones (inits/cones.py:57-143):
+    a straight centre-out line whose sample radii are those of a normalised
+    Archimedes spiral, KMAX * linspace(0, 1, Ns), laid along -z and rotated
+    onto the Fibonacci directions v_i = (cos(phi_i) r_i, sin(phi_i) r_i, z_i)
+    with z_i = linspace(-1, 1, Nc), phi_i = i pi (3 - sqrt(5)), r_i =
+    sqrt(1 - z_i^2) (tools/transforms.py:113-189).  Spoke i is therefore
+    -v_i times the radii."""
+    z = np.linspace(-1, 1, Nc)
     phi = np.pi * (3 - np.sqrt(5)) * np.arange(Nc)
-    d = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=-1)  # (Nc, 3)
+    r = np.sqrt(1 - z * z)
+    v = np.stack([np.cos(phi) * r, np.sin(phi) * r, z], axis=-1)  # (Nc, 3)
     seg = KMAX * np.linspace(0, 1, Ns)
-    return d[:, None, :] * seg[None, :, None]
+    return -v[:, None, :] * seg[None, :, None]
 
 
 def stack_of_radial_3d(Nc: int, Ns: int, Nr: int) -> np.ndarray:
@@ -153,3 +160,30 @@ def config3(n_instances: int = 32, seed: int = 0):
             "image": phantom(shape, seed=seed + i),
         })
     return out
+
+
+# Request templates of the served mix: key, share of the stream, trajectory,
+# image shape, coils (70 % 2D 256^2 radial 256 x 512 with 8-32 coils, 20 %
+# 2D 384^2 Galilean spiral 32 x 4096 with 16 coils, 10 % 3D 128^3 kooshball
+# 2048 x 512 with 8 coils).
+SERVE_MIX = [
+    ("a8", 0.175, "radial", (256, 256), 8),
+    ("a16", 0.175, "radial", (256, 256), 16),
+    ("a24", 0.175, "radial", (256, 256), 24),
+    ("a32", 0.175, "radial", (256, 256), 32),
+    ("b16", 0.2, "spiral", (384, 384), 16),
+    ("c8", 0.1, "koosh", (128, 128, 128), 8),
+]
+
+
+def serve_template(index: int):
+    """Trajectory (float32, unit), coil maps and phantom of template ``index``
+    of ``SERVE_MIX`` (seeded by the index)."""
+    key, _, kind, shape, C = SERVE_MIX[index]
+    if kind == "radial":
+        traj = radial_2d(256, 512).reshape(-1, 2)
+    elif kind == "spiral":
+        traj = spiral_2d(32, 4096, power=2).reshape(-1, 2)
+    else:
+        traj = kooshball_3d(2048, 512).reshape(-1, 3)
+    return traj.astype(np.float32), coil_maps(shape, C, seed=index), phantom(shape, seed=index)

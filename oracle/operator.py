@@ -82,6 +82,27 @@ class NDFTOperator:
         return self.adj(self.op(x))
 
 
+class EsOperator(NDFTOperator):
+    """The same operator semantics with the FP64 CPU ES-kernel NUFFT of
+    ``oracle/esnufft.py`` (eps 1e-6, about 1e-6 from the exact NDFT) in
+    place of the exact sum, for sizes where the NDFT would take hours."""
+
+    def __init__(self, samples, shape, n_coils=1, n_batchs=1, smaps=None, density=None,
+                 eps=1e-6, nthreads=None):
+        super().__init__(samples, shape, n_coils=n_coils, n_batchs=n_batchs, smaps=smaps,
+                         density=density)
+        from . import esnufft
+
+        self._es = esnufft.EsNufft(self.samples * (2 * np.pi), self.shape, eps=eps,
+                                   dtype=np.float64, nthreads=nthreads)
+
+    def _t2(self, x):
+        return self._es.type2(np.asarray(x, dtype=np.complex128).reshape(self.shape))
+
+    def _t1(self, c):
+        return self._es.type1(np.asarray(c, dtype=np.complex128).reshape(-1))
+
+
 def power_method(max_iter, gram, x):
     """base.py:1155-1221 with numpy norms; returns (norm, x)."""
     x = np.array(x, dtype=np.complex128)

@@ -149,3 +149,47 @@ def test_lsqr_matches_reference(gpu_pkg, name):
         kw["x0"] = g[f"{name}__x0"].astype(np.complex64)
     x = op.pinv_solver(g[f"{name}__ksp"].astype(np.complex64), **kw)
     assert rel_l2(x, g[f"{name}__x"]) < 1e-4
+
+
+CG_CASES = ["cg_sense", "cg_density", "cg_damp", "cg_calib", "cg_3d"]
+
+
+def _cg_golden():
+    from pathlib import Path
+
+    return np.load(Path(__file__).resolve().parent / "golden" / "cg_golden.npz")
+
+
+def _cg_operator(gpu_pkg, g, name):
+    shape = tuple(int(v) for v in g[f"{name}__shape"])
+    smaps = g[f"{name}__smaps"].astype(np.complex64) if f"{name}__smaps" in g else None
+    dens = g[f"{name}__density"].astype(np.float32) if f"{name}__density" in g else False
+    C, B = int(g[f"{name}__n_coils"]), int(g[f"{name}__n_batchs"])
+    return gpu_pkg.MRIGB300(g[f"{name}__samples"].astype(np.float32), shape, n_coils=C, n_batchs=B,
+                            smaps=smaps, density=dens, squeeze_dims=False)
+
+
+@pytest.mark.parametrize("name", CG_CASES)
+def test_lipschitz_matches_reference(gpu_pkg, name):
+    # tests/golden/cg_golden.npz: the reference's power_method on its FP64
+    # NDFT backend from the GPU backends' seeded start vector
+    g = _cg_golden()
+    op = _cg_operator(gpu_pkg, g, name)
+    np.random.seed(int(g[f"{name}__seed"]))
+    L = op.get_lipschitz_cst(max_iter=10)
+    L_ref = float(g[f"{name}__lipschitz"])
+    assert abs(L - L_ref) / L_ref < 1e-4, (L, L_ref)
+
+
+@pytest.mark.parametrize("name", CG_CASES)
+def test_cg_matches_reference(gpu_pkg, name):
+    # tests/golden/cg_golden.npz: the reference's cg (extras/optim.py:801-902,
+    # 10 iterations) on its FP64 NDFT backend, same seed
+    g = _cg_golden()
+    op = _cg_operator(gpu_pkg, g, name)
+    kw = {"damp": float(g[f"{name}__damp"]), "max_iter": 10}
+    if f"{name}__x0" in g:
+        kw["x0"] = g[f"{name}__x0"].astype(np.complex64)
+    np.random.seed(int(g[f"{name}__seed"]))
+    x = op.pinv_solver(g[f"{name}__ksp"].astype(np.complex64), optim="cg", **kw)
+    assert rel_l2(x, g[f"{name}__x"]) < 1e-4

@@ -170,3 +170,29 @@ def test_offres_factorisations_match_reference(pkg, name, method):
     prod = np.einsum("kl,l...->k...", B, Cm)
     prodg = np.einsum("kl,l...->k...", Bg, Cg)
     assert rel_l2(prod, prodg) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["cg_sense", "cg_density", "cg_damp", "cg_calib", "cg_3d"])
+def test_oracle_cg_and_power_method_match_reference(name):
+    """The oracle's power method and CG against the reference's own
+    (``tests/golden/cg_golden.npz``, made by ``make_cg_golden.py``)."""
+    from pathlib import Path
+
+    from oracle import operator as oop
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "cg_golden.npz")
+    shape = tuple(int(v) for v in g[f"{name}__shape"])
+    s = g[f"{name}__samples"]
+    smaps = g[f"{name}__smaps"] if f"{name}__smaps" in g else None
+    dens = g[f"{name}__density"] if f"{name}__density" in g else None
+    C, B = int(g[f"{name}__n_coils"]), int(g[f"{name}__n_batchs"])
+    np.random.seed(int(g[f"{name}__seed"]))
+    x0 = 1j * np.random.random(shape).astype(np.complex128)
+    x0 += np.random.random(shape).astype(np.complex128)
+    L, _ = oop.power_method(10, oop.NDFTOperator(s, shape, density=dens).gram, x0.reshape(1, 1, *shape))
+    assert abs(L - float(g[f"{name}__lipschitz"])) <= 1e-10 * L
+    op = oop.NDFTOperator(s, shape, n_coils=C, n_batchs=B, smaps=smaps, density=dens)
+    xp = g[f"{name}__x0"] if f"{name}__x0" in g else None
+    x = oop.cg(op, g[f"{name}__ksp"], L, max_iter=10, damp=float(g[f"{name}__damp"]), x0=xp)
+    ref = g[f"{name}__x"]
+    assert np.linalg.norm(x.reshape(ref.shape) - ref) <= 1e-10 * np.linalg.norm(ref)
