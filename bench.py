@@ -939,34 +939,51 @@ def run_c5(args):
     srv.prewarm(stream_reqs)
     done = srv.run(stream_reqs, realtime=True)
     stream = ReconServer.stats(done)
-    # saturated: every request present at t = 0
+    stream["ledger_peak_bytes"] = srv.ledger.peak
+    # saturated: every request present at t = 0, served with both iteration
+    # forms and run through the plain per-call backend with both
     nsat = args.saturated
     sat_reqs = make(nsat, np.zeros(nsat))
-    srv2 = ReconServer(hbm_budget_bytes=150e9, max_active=32)
-    srv2.prewarm(sat_reqs)
-    sampler = ClockSampler(0)
-    sampler.start()
-    t0 = time.perf_counter()
-    srv2.run(sat_reqs, realtime=False)
-    served_s = time.perf_counter() - t0
-    served_clk = sampler.stop()
+
+    def served(gram):
+        reqs = [ReconRequest(rid=r.rid, samples=r.samples, shape=r.shape, kspace=r.kspace,
+                             smaps=r.smaps, seed=r.seed, traj_key=r.traj_key, smaps_key=r.smaps_key)
+                for r in sat_reqs]
+        srv2 = ReconServer(hbm_budget_bytes=150e9, max_active=32, gram=gram)
+        srv2.prewarm(reqs)
+        ReconServer(max_active=32, gram=gram).run(make(len(tpl), np.zeros(len(tpl))), realtime=False)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(0)
+        sampler.start()
+        t0 = time.perf_counter()
+        srv2.run(reqs, realtime=False)
+        dt = time.perf_counter() - t0
+        return dt, sampler.stop(), srv2.ledger.peak
+
+    served_s, served_clk, peak_bytes = served("toeplitz")
+    served_nufft_s, served_nufft_clk, _ = served("nufft")
     # plain per-call backend on the same requests (host-synchronised CG loop)
     ops = {}
     for t in tpl:  # the plain backend's operators exist before the requests arrive
         ops[t["key"]] = pkg.MRIGB300(t["samples"], t["shape"], n_coils=t["smaps"].shape[0],
                                      smaps=t["smaps"], device=0)
         ops[t["key"]].pinv_solver(t["kspace"].to(dev), optim="cg", max_iter=2)
+        ops[t["key"]].pinv_solver(t["kspace"].to(dev), optim="cg", max_iter=2, toeplitz=True)
     torch.cuda.synchronize()
-    sampler = ClockSampler(0)
-    sampler.start()
-    t0 = time.perf_counter()
-    for r in sat_reqs:
-        key = r.traj_key
-        np.random.seed(r.seed)
-        ops[key].pinv_solver(r.kspace.to(dev, non_blocking=True), optim="cg", max_iter=10)
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
-    plain_clk = sampler.stop()
+
+    def plain(toeplitz):
+        sampler = ClockSampler(0)
+        sampler.start()
+        t0 = time.perf_counter()
+        for r in sat_reqs:
+            np.random.seed(r.seed)
+            ops[r.traj_key].pinv_solver(r.kspace.to(dev, non_blocking=True), optim="cg", max_iter=10,
+                                        toeplitz=toeplitz)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, sampler.stop()
+
+    plain_s, plain_clk = plain(False)
+    plain_toep_s, plain_toep_clk = plain(True)
     line = {
         "metric": "served CG reconstructions: p50/p99 latency (ms) and recon/s",
         "value": nsat / served_s, "unit": "recon/s", "n_gpus": 1, "steps": nsat, "warmup": len(tpl) * 2,
@@ -977,10 +994,19 @@ def run_c5(args):
                                "2048x512 8 coils; CG 10 iterations; 150 GB budget"
                                % (args.rate, args.duration), "max_active": 32},
         "stream": stream,
-        "saturated": {"requests": nsat, "served_recon_per_s": nsat / served_s,
-                      "plain_per_call_recon_per_s": nsat / plain_s,
-                      "speedup": plain_s / served_s,
-                      "served_clocks": served_clk, "plain_clocks": plain_clk},
+        "saturated": {
+            "requests": nsat,
+            "served_toeplitz_recon_per_s": nsat / served_s,
+            "served_nufft_recon_per_s": nsat / served_nufft_s,
+            "plain_per_call_nufft_recon_per_s": nsat / plain_s,
+            "plain_per_call_toeplitz_recon_per_s": nsat / plain_toep_s,
+            "speedup_served_vs_plain": plain_s / served_s,
+            "speedup_batching_only_toeplitz": plain_toep_s / served_s,
+            "speedup_batching_only_nufft": plain_s / served_nufft_s,
+            "speedup_toeplitz_only_plain": plain_s / plain_toep_s,
+            "ledger_peak_bytes": peak_bytes,
+            "served_clocks": served_clk, "served_nufft_clocks": served_nufft_clk,
+            "plain_clocks": plain_clk, "plain_toeplitz_clocks": plain_toep_clk},
     }
     print(json.dumps(line), flush=True)
 

@@ -107,6 +107,7 @@ class MRIGB300(_Base):
         self.squeeze_dims = squeeze_dims
         self._isign = -1
         self._toep = None
+        self._toep_unweighted = None
         self._toeplitz_kernel = None
         self.dtype = np.float32
         self._set_samples(samples)
@@ -148,6 +149,7 @@ class MRIGB300(_Base):
         self._set_samples(new_samples, unsafe=unsafe)
         self._plan.setpts(self._samples_d)
         self._toep = None
+        self._toep_unweighted = None
         self._toeplitz_kernel = None
         self.compute_density(self._density_method)
 
@@ -383,6 +385,7 @@ class MRIGB300(_Base):
             from .plan import ToeplitzKernel
 
             self._toep = ToeplitzKernel(self._plan, self._density)
+            self._toep_weighted = self._density is not None
         return self._toep
 
     def compute_toeplitz_kernel(self):
@@ -428,13 +431,27 @@ class MRIGB300(_Base):
         return MRINufftAutoGrad(self, wrt_data=wrt_data, wrt_traj=wrt_traj, paired_batch=paired_batch)
 
     # ------------------------------------------------------------- solvers
-    def get_lipschitz_cst(self, max_iter=10, **kwargs):
+    def get_lipschitz_cst(self, max_iter=10, toeplitz=False, **kwargs):
         """Largest eigenvalue of A^H A (single coil, no maps, with density)
-        by the power method of base.py:1155-1221 with FP64 norms."""
+        by the power method of base.py:1155-1221 with FP64 norms, from the
+        GPU backends' start vector (cufinufft.py:1239-1279).  ``toeplitz``
+        (an option of this backend) applies A^H W A through the Toeplitz
+        embedding."""
         x = 1j * np.random.random(self.shape).astype(np.complex64)
         x += np.random.random(self.shape).astype(np.complex64)
         x = torch.from_numpy(x).to(self.device)
-        return power_method(max_iter, self, x)
+        return power_method(max_iter, self, x, toeplitz=toeplitz)
+
+    def _unweighted_toeplitz(self):
+        """Toeplitz embedding of A^H A without density (CG iterations run
+        with density disabled, extras/optim.py:838-842)."""
+        if self._toep is not None and not self._toep_weighted:
+            return self._toep
+        if self._toep_unweighted is None:
+            from .plan import ToeplitzKernel
+
+            self._toep_unweighted = ToeplitzKernel(self._plan, None)
+        return self._toep_unweighted
 
     def pinv_solver(self, kspace_data, optim="lsqr", **kwargs):
         """Least-squares reconstruction (base.py:667-690).  ``optim="lsqr"``
@@ -494,7 +511,7 @@ class MRIGB300(_Base):
         )
 
 
-def power_method(max_iter, operator: MRIGB300, x: torch.Tensor):
+def power_method(max_iter, operator: MRIGB300, x: torch.Tensor, toeplitz=False):
     """Power iteration for the Lipschitz constant on the device, restating
     ``operators/base.py:1155-1221`` on a single-coil, map-free copy of the
     operator configuration (base.py:647-665).  Returns a host float."""
@@ -510,7 +527,10 @@ def power_method(max_iter, operator: MRIGB300, x: torch.Tensor):
         x_new_norm = x_norm
         i = 0
         for i in range(max_iter):  # noqa: B007
-            x_new = operator._adj_device(operator._op_device(x)).reshape(1, *operator.shape)
+            if toeplitz:
+                x_new = operator._gram_device(x).reshape(1, *operator.shape)
+            else:
+                x_new = operator._adj_device(operator._op_device(x)).reshape(1, *operator.shape)
             x_new_norm = float(norm2_f64(x_new).sqrt())
             x_new = x_new / x_new_norm
             if abs(x_norm - x_new_norm) < 1e-6:

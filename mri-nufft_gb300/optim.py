@@ -44,11 +44,17 @@ def scaled_dcp(operator, ksp: torch.Tensor) -> torch.Tensor:
 
 
 def cg(operator, kspace_data, damp=0.0, x0=None, x_init=None, max_iter=10, tol=1e-4,
-       progressbar=False, callback=None):
-    """Nonlinear CG with fixed step 1/L; returns an image in the input's array type."""
+       progressbar=False, callback=None, toeplitz=False):
+    """Nonlinear CG with fixed step 1/L; returns an image in the input's array type.
+
+    ``toeplitz=True`` (an option of this backend, off by default) takes the
+    power method and the gradients A^H A x - A^H y from the Toeplitz
+    embedding of the Gram operator (A^H y from one adjoint at the start)
+    instead of a forward and an adjoint NUFFT per iteration; the iteration
+    is otherwise the same."""
     like = _array.interface_of(kspace_data)
     dev = operator.device
-    L = float(operator.get_lipschitz_cst())
+    L = float(operator.get_lipschitz_cst(toeplitz=toeplitz))
     y = _array.to_tensor(kspace_data, dev, torch.complex64).reshape(operator.ksp_full_shape)
     old_density = None
     if operator.uses_density:
@@ -64,9 +70,19 @@ def cg(operator, kspace_data, damp=0.0, x0=None, x_init=None, max_iter=10, tol=1
             image = _array.to_tensor(x_init, dev, torch.complex64).reshape(shape)
         x0_t = None if x0 is None else _array.to_tensor(x0, dev, torch.complex64).reshape(shape)
         velocity = torch.zeros_like(image)
+        if toeplitz:
+            gram = operator._unweighted_toeplitz()
+            rhs = operator._adj_device(y, density=False)
+            B, C = operator.n_batchs, operator.n_coils
 
         def grad_of(img):
-            g = dc(operator, img, y)
+            if toeplitz:
+                x = img.reshape(B, *operator.shape) if operator.uses_sense else img.reshape(B * C, *operator.shape)
+                g = torch.empty(shape, dtype=torch.complex64, device=dev)
+                gram.apply(x.contiguous(), operator._smaps, g, B, C, operator.inv_norm_factor ** 2)
+                g = g - rhs.reshape(shape)
+            else:
+                g = dc(operator, img, y)
             if damp:
                 g = g + damp * (img - x0_t if x0_t is not None else img)
             return g

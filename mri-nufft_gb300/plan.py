@@ -235,6 +235,13 @@ class ToeplitzKernel:
         _lib.check(self.lib.gbn_toep_plan(self._h, ctypes.byref(h)), "gbn_toep_plan")
         return h
 
+    def inner_device_bytes(self) -> int:
+        """Device bytes of the embedding (circulant grids and kernel spectrum)."""
+        b = ctypes.c_int64()
+        _lib.check(self.lib.gbn_plan_device_bytes(self._inner(), ctypes.byref(b)),
+                   "gbn_plan_device_bytes")
+        return b.value
+
     def kernel(self) -> torch.Tensor:
         """The real kernel spectrum, shape ``grid`` (device, float32)."""
         out = torch.empty(self.grid, dtype=torch.float32, device=self.device)

@@ -20,13 +20,18 @@ and coil counts as they arrive:
   the CG step (Polak-Ribiere beta with numpy's complex ``max(0, beta)``, the
   ``tol`` early exit) and their FP64 reductions run on the device
   (``gbn_power_step``, ``gbn_cg_update``, ``gbn_dotu_f64``, ``gbn_norm2_f64``);
-* FFT-only iterations: the power method and the CG gradients use the
-  Toeplitz embedding of the Gram operator (``gbn_toep_*``; A^H W A x as a
-  circulant convolution on a 2N grid), so an iteration runs FFTs and one
+* FFT-only iterations (default): the power method and the CG gradients use
+  the Toeplitz embedding of the Gram operator (``gbn_toep_*``; A^H W A x as
+  a circulant convolution on a 2N grid), so an iteration runs FFTs and one
   multiply per coil instead of a spread and an interpolation.  The CG
   gradient A^H A x - A^H y takes A^H y from one adjoint transform at the
   start.  The Toeplitz kernel of a trajectory is built once and pooled with
-  its sorted plan.
+  its sorted plan.  ``gram="nufft"`` keeps the NUFFT data-consistency
+  iterations of ``pinv_solver(optim="cg")`` instead;
+* HBM budget: an :class:`HbmLedger` charges every resident sorted
+  trajectory (pooled or in use), every resident coil map and the state of
+  every admitted request; requests wait, and idle pooled trajectories are
+  freed, so that the total never exceeds the budget.
 
 Each result equals the same request run alone (and ``MRIGB300.pinv_solver``
 with the same power-method start vector) up to float rounding.
@@ -86,39 +91,106 @@ def start_vector(shape, seed):
     return x
 
 
-def request_bytes(shape, M, C, eps=1e-6):
-    """Device bytes of one admitted request: plan (fine grids, sort tables),
-    Toeplitz kernel and its grids, coil maps, k-space, CG / power-method
-    vectors."""
+def plan_set_bytes(shape, M, C, eps=1e-6):
+    """Device bytes of one resident sorted trajectory for C coils: the NUFFT
+    plan (C fine grids, sorted coordinates, permutation, bin and subproblem
+    tables) and its Toeplitz embedding (C circulant grids and the kernel
+    spectrum).  An upper bound of what the library allocates for them."""
     G = fine_cells(shape, eps)
-    N = int(np.prod(shape))
     d = len(shape)
-    plan = 8 * C * G + M * (12 + 4 * d) + 8 * C * M
-    toep = 8 * C * G + 4 * G
-    data = 8 * C * N + 8 * C * M + 4 * M
-    state = 8 * N * 8
-    return int(plan + toep + data + state)
+    plan = 8 * C * G + M * (16 + 4 * d) + 64 * (G // 64 + 1024) + (1 << 20)
+    toep = 8 * C * G + 4 * G + (1 << 20)
+    return int(plan + toep)
+
+
+def smaps_bytes(shape, C):
+    return int(8 * C * int(np.prod(shape)))
+
+
+def solve_bytes(shape, M, C, density=False, cached_smaps=False, gram="toeplitz", eps=1e-6):
+    """Device bytes of one admitted request besides its sorted trajectory:
+    coil maps (unless resident), k-space, density and, for a request with
+    density, the weighted Toeplitz kernel of its power method; the CG and
+    power-method vectors."""
+    N = int(np.prod(shape))
+    b = 8 * C * M + 8 * N * 12 + 8 * M
+    if not cached_smaps:
+        b += smaps_bytes(shape, C)
+    if density:
+        b += 4 * M
+        if gram == "toeplitz":
+            b += 8 * C * fine_cells(shape, eps) + 4 * fine_cells(shape, eps)
+    return int(b)
+
+
+def request_bytes(shape, M, C, eps=1e-6):
+    """Device bytes of a request that brings its own sorted trajectory and
+    coil maps (the most it can add to the device)."""
+    return plan_set_bytes(shape, M, C, eps) + solve_bytes(shape, M, C, eps=eps)
+
+
+class HbmLedger:
+    """Device bytes a server holds, against its HBM budget.
+
+    ``resident`` counts what outlives a request: every sorted trajectory with
+    its Toeplitz embedding that the server has built (admitted or waiting in
+    the pool) and the coil maps kept by key; ``active`` the per-request
+    state of admitted requests.  Admission and pre-building only proceed
+    when ``resident + active + need`` stays within the budget, so the sum
+    never exceeds it (``peak`` records the largest total seen)."""
+
+    def __init__(self, budget):
+        self.budget = float(budget)
+        self.resident = 0
+        self.active = 0
+        self.peak = 0
+
+    @property
+    def total(self):
+        return self.resident + self.active
+
+    def fits(self, need):
+        return self.total + need <= self.budget
+
+    def _mark(self):
+        self.peak = max(self.peak, self.total)
+
+    def add_resident(self, b):
+        self.resident += int(b)
+        self._mark()
+
+    def drop_resident(self, b):
+        self.resident -= int(b)
+
+    def add_active(self, b):
+        self.active += int(b)
+        self._mark()
+
+    def drop_active(self, b):
+        self.active -= int(b)
 
 
 class _PlanSet:
-    """A sorted trajectory: the NUFFT plan and the Toeplitz embedding of its
-    unweighted Gram operator."""
+    """A sorted trajectory: the NUFFT plan and, for the Toeplitz iterations,
+    the Toeplitz embedding of its unweighted Gram operator."""
 
-    def __init__(self, plan):
+    def __init__(self, plan, gram, nbytes):
         from .plan import ToeplitzKernel
 
         self.plan = plan
-        self.toep = ToeplitzKernel(plan, None)
+        self.toep = ToeplitzKernel(plan, None) if gram == "toeplitz" else None
+        self.bytes = int(nbytes)
 
 
 class _Solve:
     """Device state and unit generator of one admitted request."""
 
-    def __init__(self, server, req, pset, stream):
+    def __init__(self, server, req, pset, stream, nbytes):
         self.server, self.req, self.stream = server, req, stream
         self.pset, self.plan = pset, pset.plan
         self.dev = server.device
         self.lib = server.lib
+        self.gram = server.gram
         shape = tuple(int(v) for v in req.shape)
         self.shape = shape
         C = req.n_coils
@@ -132,7 +204,7 @@ class _Solve:
             self.x0 = torch.from_numpy(x0).to(self.dev)
         self.M = self.y.shape[1]
         self.scale = 1.0 / float(np.sqrt(np.prod(shape) * 2 ** len(shape)))
-        self.bytes = request_bytes(shape, self.M, C, server.eps)
+        self.bytes = int(nbytes)
         self._sth = None
         self.gen = self._units()
         self.event = None
@@ -145,6 +217,15 @@ class _Solve:
     def _ck(self, status, what):
         _lib.check(status, what)
 
+    def _dots(self, gnew, grad, st, n):
+        """state[0..6] of gbn_cg_update: dot(g_new, g_new), dot(g_new, g),
+        dot(g, g) (non-conjugating) and |g_new|^2, on the device."""
+        sth = self._st()
+        self._ck(self.lib.gbn_dotu_f64(_ptr(gnew), _ptr(gnew), n, 0, _ptr(st[0:2]), sth), "dot")
+        self._ck(self.lib.gbn_dotu_f64(_ptr(gnew), _ptr(grad), n, 0, _ptr(st[2:4]), sth), "dot")
+        self._ck(self.lib.gbn_dotu_f64(_ptr(grad), _ptr(grad), n, 0, _ptr(st[4:6]), sth), "dot")
+        self._ck(self.lib.gbn_norm2_f64(_ptr(gnew), n, _ptr(st[6:7]), sth), "norm2")
+
     def _units(self):
         dev, plan, shape, C = self.dev, self.plan, self.shape, self.C
         n = int(np.prod(shape))
@@ -155,9 +236,10 @@ class _Solve:
         c64 = dict(dtype=torch.complex64, device=dev)
         f64 = dict(dtype=torch.float64, device=dev)
         scale2 = self.scale * self.scale
+        toeplitz = self.gram == "toeplitz"
         toep = self.pset.toep
         toep_w = toep
-        if self.dens is not None:
+        if toeplitz and self.dens is not None:
             from .plan import ToeplitzKernel
 
             toep_w = ToeplitzKernel(plan, self.dens)  # A^H D A of the power method
@@ -173,7 +255,14 @@ class _Solve:
         yield
         sth = self._st()
         for _ in range(10):
-            toep_w.power_iter(x, xn, pst, L, scale2, sth)
+            if toeplitz:
+                toep_w.power_iter(x, xn, pst, L, scale2, sth)
+            else:
+                plan.op(x, None, ktmp, 1, 1, self.scale)
+                plan.adj(ktmp, self.dens, None, xn, 1, 1, self.scale)
+                self._ck(self.lib.gbn_norm2_f64(_ptr(xn), n, _ptr(pst), sth), "norm2")
+                self._ck(self.lib.gbn_power_step(n, _ptr(xn), _ptr(x), _ptr(pst), _ptr(L), sth),
+                         "power step")
             yield
         self.L = L
         # -- start image: scaled density-compensated adjoint (optim.py:151-165)
@@ -189,22 +278,31 @@ class _Solve:
             self._ck(self.lib.gbn_scale_ratio(nimg, _ptr(image), _ptr(nrm[0:1]), _ptr(nrm[1:2]),
                                               self._st()), "scale")
             yield
-        # -- CG iterations without density (optim.py:838-842); the gradient
-        # A^H (A x - y) = A^H A x - A^H y with A^H y from one adjoint
-        rhs = torch.empty(img_shape, **c64)
-        plan.adj(y, None, self.smaps, rhs, 1, C, self.scale)
+        # -- CG iterations without density (optim.py:838-842)
         grad = torch.empty(img_shape, **c64)
         gnew = torch.empty(img_shape, **c64)
         xin = image.reshape(1 if sense else C, *shape)
-        toep.apply(xin, self.smaps, grad, 1, C, scale2)
-        grad -= rhs
+        if toeplitz:
+            # A^H (A x - y) = A^H A x - A^H y with A^H y from one adjoint
+            rhs = torch.empty(img_shape, **c64)
+            plan.adj(y, None, self.smaps, rhs, 1, C, self.scale)
+            toep.apply(xin, self.smaps, grad, 1, C, scale2)
+            grad -= rhs
+        else:
+            plan.dc(xin, y, None, self.smaps, grad, 1, C, self.scale)
         velocity = grad / L
         image -= velocity
         st = torch.zeros(8, **f64)
         yield
         tol = float(self.req.tol)
         for _ in range(self.req.max_iter):
-            toep.cg_iter(image, self.smaps, rhs, grad, gnew, velocity, st, L, 1, C, scale2, tol, sth)
+            if toeplitz:
+                toep.cg_iter(image, self.smaps, rhs, grad, gnew, velocity, st, L, 1, C, scale2, tol, sth)
+            else:
+                plan.dc(xin, y, None, self.smaps, gnew, 1, C, self.scale)
+                self._dots(gnew, grad, st, nimg)
+                self._ck(self.lib.gbn_cg_update(nimg, _ptr(gnew), _ptr(grad), _ptr(velocity),
+                                                _ptr(image), _ptr(st), _ptr(L), tol, sth), "cg update")
             yield
         self.image = image
         self.event = torch.cuda.Event()
@@ -221,11 +319,22 @@ class _Solve:
 
 
 class ReconServer:
-    """Continuous-batching CG reconstruction service on one GPU."""
+    """Continuous-batching CG reconstruction service on one GPU.
 
-    def __init__(self, hbm_budget_bytes=150e9, max_active=32, device=None, eps=1e-6):
+    ``gram="toeplitz"`` (default) runs the power method and the CG gradients
+    on the Toeplitz embedding of the Gram operator; ``gram="nufft"`` runs
+    them as in ``pinv_solver(optim="cg")``, a forward and an adjoint NUFFT
+    per iteration (data consistency), with the same device-side steps.
+    Everything the server keeps on the device is charged to an
+    :class:`HbmLedger` against ``hbm_budget_bytes``."""
+
+    def __init__(self, hbm_budget_bytes=150e9, max_active=32, device=None, eps=1e-6,
+                 gram="toeplitz"):
+        if gram not in ("toeplitz", "nufft"):
+            raise ValueError("gram must be 'toeplitz' or 'nufft'")
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
-        self.budget = float(hbm_budget_bytes)
+        self.gram = gram
+        self.ledger = HbmLedger(hbm_budget_bytes)
         self.max_active = int(max_active)
         self.eps = eps
         self.lib = _lib.load()
@@ -233,37 +342,53 @@ class ReconServer:
         self.active = []
         self.finishing = []
         self.done = []
-        self.used = 0
         self.plans = defaultdict(list)   # (traj key, shape, coils) -> free sorted plans
         self.smaps_cache = {}            # smaps key -> resident coil maps
         self.rng_pool = ThreadPoolExecutor(max_workers=4)
-        self.plan_bytes = 0
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(self.max_active)]
+        self.streams = [None] * self.max_active  # created on first use
         self.free_streams = list(range(self.max_active))
         self.t0 = time.perf_counter()
+
+    @property
+    def budget(self):
+        return self.ledger.budget
+
+    def _stream(self, i):
+        if self.streams[i] is None:
+            self.streams[i] = torch.cuda.Stream(self.device)
+        return self.streams[i]
 
     def now(self):
         return time.perf_counter() - self.t0
 
+    @staticmethod
+    def _key(req):
+        shape = tuple(int(v) for v in req.shape)
+        return (req.traj_key if req.traj_key is not None else ("rid", req.rid), shape, req.n_coils)
+
+    def _pset_bytes(self, req):
+        return plan_set_bytes(tuple(req.shape), int(np.asarray(req.kspace.shape)[-1]), req.n_coils,
+                              self.eps)
+
     def prewarm(self, requests, per_key=None):
-        """Build the resident sorted plans and Toeplitz kernels that
+        """Build the resident sorted plans (and Toeplitz kernels) that
         ``requests`` will need before they arrive, so that admission never
         sorts a trajectory on a request's critical path: ``per_key`` plan sets
         per trajectory key, by default the key's share of the slots (its
-        share of ``requests`` times ``max_active``, plus 2)."""
+        share of ``requests`` times ``max_active``, plus 2).  Building stops
+        where the next plan set would not fit the HBM budget."""
         counts, first = defaultdict(int), {}
         for r in requests:
-            shape = tuple(int(v) for v in r.shape)
-            key = (r.traj_key if r.traj_key is not None else ("rid", r.rid), shape, r.n_coils)
+            key = self._key(r)
             counts[key] += 1
             first.setdefault(key, r)
         n = max(1, len(requests))
         for key, r in first.items():
             want = (int(per_key) if per_key is not None
                     else min(self.max_active, int(np.ceil(self.max_active * counts[key] / n)) + 2))
-            with torch.cuda.stream(self.streams[0]):
-                while len(self.plans[key]) < want:
-                    self.plans[key].append(self._acquire_plan(r, self.streams[0], fresh=True)[1])
+            with torch.cuda.stream(self._stream(0)):
+                while len(self.plans[key]) < want and self.ledger.fits(self._pset_bytes(r)):
+                    self.plans[key].append(self._build_plan(r, self._stream(0)))
         torch.cuda.synchronize(self.device)
 
     def submit(self, req: ReconRequest):
@@ -275,45 +400,80 @@ class ReconServer:
     def _smaps_of(self, req, C, shape):
         """Device coil maps of a request; maps with a ``smaps_key`` stay
         resident for later requests with the same key."""
-        if req.smaps_key is not None and req.smaps_key in self.smaps_cache:
+        if req.smaps_key is not None and self.smaps_cache.get(req.smaps_key) is not None:
             return self.smaps_cache[req.smaps_key]
         t = _array.to_tensor(req.smaps, self.device, torch.complex64).reshape(C, *shape)
         if req.smaps_key is not None:
-            self.smaps_cache[req.smaps_key] = t
-            self.plan_bytes += t.numel() * 8
+            self.smaps_cache[req.smaps_key] = t  # charged to the ledger at admission
         return t
 
-    def _acquire_plan(self, req, stream, fresh=False):
+    def _build_plan(self, req, stream):
         shape = tuple(int(v) for v in req.shape)
-        key = (req.traj_key if req.traj_key is not None else ("rid", req.rid), shape, req.n_coils)
-        pool = self.plans[key]
-        if pool and not fresh:
-            return key, pool.pop()
+        nbytes = self._pset_bytes(req)
         with torch.cuda.stream(stream):
             plan = NufftPlan(shape, eps=self.eps, ntrans=req.n_coils, device=self.device.index)
             s = proper_trajectory(req.samples, "pi")
             k = _array.to_tensor(s, self.device, torch.float32).reshape(-1, len(shape))
             plan.setpts(k)
-            pset = _PlanSet(plan)
-        self.plan_bytes += plan.device_bytes
-        return key, pset
+            pset = _PlanSet(plan, self.gram, nbytes)
+        self.ledger.add_resident(pset.bytes)
+        return pset
+
+    def _need(self, req):
+        """Bytes that admitting ``req`` adds: (its solver state, its coil maps
+        kept resident under their key, a sorted trajectory unless one is
+        pooled)."""
+        shape = tuple(int(v) for v in req.shape)
+        M = int(np.asarray(req.kspace.shape)[-1])
+        keep = req.smaps is not None and req.smaps_key is not None and req.smaps_key not in self.smaps_cache
+        cached = req.smaps is None or req.smaps_key is not None
+        solve = solve_bytes(shape, M, req.n_coils, density=req.density is not None,
+                            cached_smaps=cached, gram=self.gram, eps=self.eps)
+        smaps_res = smaps_bytes(shape, req.n_coils) if keep else 0
+        pset = 0 if self.plans[self._key(req)] else self._pset_bytes(req)
+        return solve, smaps_res, pset
+
+    def _evict_for(self, need, keep_key):
+        """Free pooled (idle) plan sets of other trajectories, then of the
+        request's own, until ``need`` more bytes fit."""
+        for own in (False, True):
+            for key in list(self.plans):
+                if (key == keep_key) != own:
+                    continue
+                pool = self.plans[key]
+                # the request's own pool keeps the plan set its need assumed
+                while len(pool) > int(own) and not self.ledger.fits(need):
+                    p = pool.pop()
+                    self.ledger.drop_resident(p.bytes)
+                    del p
+                if self.ledger.fits(need):
+                    return True
+        return self.ledger.fits(need)
 
     def _admit(self):
         while self.queue and self.free_streams:
             req = self.queue[0]
             if not req._x0.done():
                 break
-            need = request_bytes(tuple(req.shape), int(np.asarray(req.kspace.shape)[-1]),
-                                 req.n_coils, self.eps)
-            if (self.active or self.finishing) and self.used + need > self.budget:
+            solve_b, smaps_b, pset_b = self._need(req)
+            need = solve_b + smaps_b + pset_b
+            if not self.ledger.fits(need) and not self._evict_for(need, self._key(req)):
+                if not (self.active or self.finishing):
+                    raise RuntimeError(
+                        f"request {req.rid} needs {need} device bytes, more than the HBM budget "
+                        f"of {int(self.budget)} holds with {self.ledger.resident} resident")
                 break
             self.queue.popleft()
             si = self.free_streams.pop()
-            stream = self.streams[si]
-            key, pset = self._acquire_plan(req, stream)
-            solve = _Solve(self, req, pset, stream)
+            stream = self._stream(si)
+            key = self._key(req)
+            pset = self.plans[key].pop() if self.plans[key] else self._build_plan(req, stream)
+            if smaps_b:  # coil maps that stay resident under their key
+                self.smaps_cache[req.smaps_key] = None
+                self.ledger.add_resident(smaps_b)
+            solve = _Solve(self, req, pset, stream, solve_b)
             solve.key, solve.si = key, si
-            self.used += solve.bytes
+            self.ledger.add_active(solve.bytes)
             req.t_admit = self.now()
             self.active.append(solve)
 
@@ -324,7 +484,7 @@ class ReconServer:
                 s.req.result = s.image
                 s.req.lipschitz = s.L
                 s.req.t_done = self.now()
-                self.used -= s.bytes
+                self.ledger.drop_active(s.bytes)
                 self.plans[s.key].append(s.pset)
                 self.free_streams.append(s.si)
                 self.done.append(s.req)

@@ -84,22 +84,62 @@ def test_alone_equals_mix_equals_plain(gpu_pkg):
         assert rel_l2(alone[r.rid], x) < 1e-4
 
 
+@pytest.mark.parametrize("gram", ["toeplitz", "nufft"])
+def test_alone_equals_plain_both_grams(gpu_pkg, gram):
+    """Both served iteration forms equal the plain per-call CG (the NUFFT
+    form exactly the same arithmetic; the Toeplitz form through its own
+    option of the plain solver too)."""
+    from mrinufft_gb300.serving import ReconServer
+
+    rng = np.random.default_rng(3)
+    reqs = _requests(rng)
+    srv = ReconServer(max_active=8, gram=gram)
+    done = {r.rid: r for r in srv.run([_copy(r) for r in reqs], realtime=False)}
+    for r in reqs:
+        op = gpu_pkg.MRIGB300(r.samples, r.shape, n_coils=r.n_coils, smaps=r.smaps,
+                              density=r.density)
+        np.random.seed(r.seed)
+        x = op.pinv_solver(r.kspace, optim="cg", max_iter=10, toeplitz=gram == "toeplitz")
+        assert rel_l2(done[r.rid].result.cpu().numpy(), x) < 1e-4
+
+
 def test_budget_limits_concurrency(gpu_pkg):
-    from mrinufft_gb300.serving import ReconServer, request_bytes
+    from mrinufft_gb300.serving import ReconServer, plan_set_bytes, solve_bytes
 
     rng = np.random.default_rng(1)
     reqs = _requests(rng)[:2] * 3
     reqs = [_copy(r, rid=i) for i, r in enumerate(reqs)]
-    one = max(request_bytes(r.shape, r.kspace.shape[1], r.n_coils) for r in reqs)
-    srv = ReconServer(hbm_budget_bytes=1.5 * one, max_active=8)
+    one = max(plan_set_bytes(r.shape, r.kspace.shape[1], r.n_coils)
+              + solve_bytes(r.shape, r.kspace.shape[1], r.n_coils) for r in reqs)
+    budget = 2.5 * one
+    srv = ReconServer(hbm_budget_bytes=budget, max_active=8)
+    srv.prewarm(reqs)
+    assert srv.ledger.total <= budget
     peak = 0
-    pending = list(reqs)
-    for r in pending:
+    for r in reqs:
         srv.submit(r)
     while not srv.idle():
         srv.tick()
         peak = max(peak, len(srv.active) + len(srv.finishing))
-        assert srv.used <= 1.5 * one or len(srv.active) + len(srv.finishing) == 1
+        assert srv.ledger.total <= budget
     torch.cuda.synchronize()
     assert len(srv.done) == len(reqs)
     assert peak <= 2
+    assert srv.ledger.peak <= budget
+
+
+def test_plan_set_estimate_bounds_library_bytes(gpu_pkg):
+    """The ledger's per-trajectory charge is at least what the library
+    allocates for the plan and its Toeplitz embedding."""
+    from mrinufft_gb300.plan import NufftPlan, ToeplitzKernel
+    from mrinufft_gb300.serving import plan_set_bytes
+
+    rng = np.random.default_rng(2)
+    for r in _requests(rng):
+        k = torch.from_numpy(np.asarray(r.samples, np.float32) * np.float32(2 * np.pi)).cuda()
+        plan = NufftPlan(tuple(r.shape), eps=1e-6, ntrans=r.n_coils)
+        plan.setpts(k)
+        toep = ToeplitzKernel(plan, None)
+        inner = toep.inner_device_bytes()
+        assert plan.device_bytes + inner <= plan_set_bytes(r.shape, k.shape[0], r.n_coils)
+        del toep, plan
