@@ -45,6 +45,7 @@ struct Geom {
                       // 5: 3D quadrant streaming (8 x 8 bins)
   int interp_threads; // CTA size of the tile interp kernel (0: 128)
   int spread_cg;      // coils per pass of the streaming spreader (0: automatic)
+  int quad_minb;      // resident CTAs per SM of the 4-coil quadrant spreader (0: 4)
 };
 
 // Work table of one sorted trajectory.

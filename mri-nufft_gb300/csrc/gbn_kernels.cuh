@@ -1237,8 +1237,8 @@ __host__ __device__ constexpr size_t quad_smem_bytes(int cg) {
          (size_t)cg * kQuadRound * sizeof(float2) + (size_t)kStreamBatch * sizeof(short);
 }
 
-template <int W, int CG>
-__global__ void __launch_bounds__(kQuadThreads, 4)
+template <int W, int CG, int MINB>
+__global__ void __launch_bounds__(kQuadThreads, MINB)
 spread_quad3d_kernel(SpreadArgs a) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   float* s_w2 = reinterpret_cast<float*>(s_raw);           // [kQuadRound][8], slot order
@@ -1972,11 +1972,11 @@ cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int W, int CG>
+template <int W, int CG, int MINB = 4>
 cudaError_t launch_spread_quad_t(const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return cudaSuccess;
   const size_t smem = quad_smem_bytes(CG);
-  auto k = spread_quad3d_kernel<W, CG>;
+  auto k = spread_quad3d_kernel<W, CG, MINB>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<(unsigned)(4 * (int64_t)a.s.nsub), kQuadThreads, smem, st>>>(a);
@@ -1991,6 +1991,11 @@ inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st
   // 3D kooshball); GBN_SPREAD=stream keeps the column kernel
   if ((a.g.method_spread == 0 || a.g.method_spread == 5) && a.g.bs[0] == 8 && a.g.bs[1] == 8) {
     if (a.g.w == 7) {
+      // 8 coils per pass (two CTAs of 255 registers per SM) for 8 or more
+      // transforms when GBN_SPREAD_CG=8; 4 coils at 3 CTAs per SM when
+      // GBN_QUAD_MINB=3
+      if (a.g.spread_cg == 8 && a.ntr >= 8) return launch_spread_quad_t<7, 8, 2>(a, st);
+      if (cg == 4 && a.g.quad_minb == 3) return launch_spread_quad_t<7, 4, 3>(a, st);
       if (cg == 4) return launch_spread_quad_t<7, 4>(a, st);
       return cg == 2 ? launch_spread_quad_t<7, 2>(a, st) : launch_spread_quad_t<7, 1>(a, st);
     }

@@ -76,3 +76,20 @@ def test_variant_matches_oracle(gpu_pkg, monkeypatch, env, dim, sense):
     assert rel_l2(op.op(x), ref.op(x)) < TOL
     assert rel_l2(op.adj_op(y), ref.adj(y)) < TOL
     assert rel_l2(op.data_consistency(x, y), ref.dc(x, y)) < TOL
+
+
+@pytest.mark.parametrize("env", [{}, {"GBN_SPREAD_CG": "8"}, {"GBN_QUAD_MINB": "3"}], ids=_ids)
+@pytest.mark.parametrize("C", [8, 9, 17])
+def test_quadrant_spreader_coil_groups(gpu_pkg, monkeypatch, env, C):
+    """The 3D quadrant spreader with 8 coils per pass or 3 CTAs per SM, on
+    coil counts that leave a partial last pass."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    rng = np.random.default_rng(C)
+    shape, M = (24, 20, 16), 5000
+    k = np.concatenate([rng.uniform(-0.5, 0.5, (M // 2, 3)),
+                        np.clip(rng.normal(0, 0.06, (M // 2, 3)), -0.5, 0.4999)]).astype(np.float32)
+    y = (rng.standard_normal((1, C, M)) + 1j * rng.standard_normal((1, C, M))).astype(np.complex64)
+    op = gpu_pkg.MRIGB300(k, shape, n_coils=C, squeeze_dims=False)
+    ref = NDFTOperator(k.astype(np.float64), shape, n_coils=C)
+    assert rel_l2(op.adj_op(y), ref.adj(y)) < TOL
