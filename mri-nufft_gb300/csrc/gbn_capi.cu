@@ -612,6 +612,7 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
                         : std::strcmp(e, "stream") == 0 ? 3
                         : std::strcmp(e, "rows") == 0   ? 4
                         : std::strcmp(e, "quad") == 0   ? 5
+                        : std::strcmp(e, "mma") == 0    ? 6
                                                         : 0;
     for (int d = 0; d < 3; ++d) {
       if (d < dim) {

@@ -42,10 +42,11 @@ struct Geom {
                       // 5: 3D tile warp-cooperative, 6: tiles
   int method_spread;  // 0: automatic, 1: global atomics, 2: warp-cooperative atomics,
                       // 3: 3D column streaming, 4: 3D bin-tile rows,
-                      // 5: 3D quadrant streaming (8 x 8 bins)
+                      // 5: 3D quadrant streaming (8 x 8 bins),
+                      // 6: 3D quadrant tiles on the tensor cores (8 x 8 bins, w = 7)
   int interp_threads; // CTA size of the tile interp kernel (0: 128)
   int spread_cg;      // coils per pass of the streaming spreader (0: automatic)
-  int quad_minb;      // resident CTAs per SM of the 4-coil quadrant spreader (0: 4)
+  int quad_minb;      // resident CTAs per SM of the 4-coil quadrant spreader (0: 3)
 };
 
 // Work table of one sorted trajectory.
@@ -210,7 +211,8 @@ inline bool rows_fit(const Geom& g) {
 // header, use the column-streaming spreaders (an 8-cell register window
 // along the last axis).
 inline bool stream_fit(const Geom& g) {
-  if (g.w > 7 || !(g.method_spread == 0 || g.method_spread == 3 || g.method_spread == 5))
+  if (g.w > 7 || !(g.method_spread == 0 || g.method_spread == 3 || g.method_spread == 5 ||
+                   g.method_spread == 6))
     return false;
   if (g.dim == 2) return g.pd[0] <= 32 && g.nf[1] <= 16000;
   return g.dim == 3 && g.bs[0] <= 15 && g.bs[1] <= 15 && g.pd[0] <= 16 && g.pd[1] <= 16 &&

@@ -1983,20 +1983,29 @@ cudaError_t launch_spread_quad_t(const SpreadArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+}  // namespace gbn
+
+#include "gbn_mma_spread.cuh"
+
+namespace gbn {
+
 // a.s is the column-chunk table (sub_bin = column index)
 inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st) {
   int cg = a.ntr >= 3 ? 4 : a.ntr;
   if (a.g.spread_cg == 1 || a.g.spread_cg == 2 || a.g.spread_cg == 4) cg = imin(cg, a.g.spread_cg);
   // 8 x 8 bins: quadrant CTAs (measured 7 % faster than whole columns on the
   // 3D kooshball); GBN_SPREAD=stream keeps the column kernel
+  if (a.g.method_spread == 6 && a.g.w == 7 && a.g.bs[0] == 8 && a.g.bs[1] == 8)
+    return launch_spread_mma3d(a, st);
   if ((a.g.method_spread == 0 || a.g.method_spread == 5) && a.g.bs[0] == 8 && a.g.bs[1] == 8) {
     if (a.g.w == 7) {
-      // 8 coils per pass (two CTAs of 255 registers per SM) for 8 or more
-      // transforms when GBN_SPREAD_CG=8; 4 coils at 3 CTAs per SM when
-      // GBN_QUAD_MINB=3
+      // 4 coils per pass at 3 CTAs per SM (170 registers, no spills;
+      // measured 7.08 against 7.63 ms at 4 CTAs per SM, whose 128-register
+      // cap spills, on the 16-coil 3D kooshball); GBN_QUAD_MINB=4 keeps 4
+      // CTAs; GBN_SPREAD_CG=8 runs 8 coils per pass at 2 CTAs per SM (7.50 ms)
       if (a.g.spread_cg == 8 && a.ntr >= 8) return launch_spread_quad_t<7, 8, 2>(a, st);
-      if (cg == 4 && a.g.quad_minb == 3) return launch_spread_quad_t<7, 4, 3>(a, st);
-      if (cg == 4) return launch_spread_quad_t<7, 4>(a, st);
+      if (cg == 4 && a.g.quad_minb == 4) return launch_spread_quad_t<7, 4, 4>(a, st);
+      if (cg == 4) return launch_spread_quad_t<7, 4, 3>(a, st);
       return cg == 2 ? launch_spread_quad_t<7, 2>(a, st) : launch_spread_quad_t<7, 1>(a, st);
     }
     if (cg == 4) return launch_spread_quad_t<0, 4>(a, st);

@@ -138,6 +138,7 @@ def main(ref_src):
     out["radial__shape"] = np.array(shape)
     out["radial__calib_width"] = np.array(cw)
     out["radial__kernel_width"] = np.array(kw)
+    out["radial__center_img"] = np.asarray(img_c)
     out["radial__central"] = central
     out["radial__maps"] = sm
     out["radial__eig"] = eig

@@ -3,7 +3,8 @@ FP64 NDFT oracle.
 
 ``gbn_plan_create`` reads tuning overrides from the environment: the spread
 kernel (``GBN_SPREAD``: per-sample global atomics, warp-cooperative atomics,
-column streaming, bin-tile rows, quadrant streaming), the interpolation kernel
+column streaming, bin-tile rows, quadrant streaming, quadrant tiles on the
+tensor cores), the interpolation kernel
 (``GBN_INTERP``: direct, double-buffered tiles, warp-cooperative, tile +
 warp-cooperative, tiles), coils per pass (``GBN_INTERP_CG``,
 ``GBN_SPREAD_CG``), the interp CTA size (``GBN_INTERP_THREADS``), the bin
@@ -27,7 +28,7 @@ TOL = 1e-4
 VARIANTS = [
     {},
     {"GBN_SPREAD": "gm"}, {"GBN_SPREAD": "wc"}, {"GBN_SPREAD": "stream"},
-    {"GBN_SPREAD": "rows"}, {"GBN_SPREAD": "quad"},
+    {"GBN_SPREAD": "rows"}, {"GBN_SPREAD": "quad"}, {"GBN_SPREAD": "mma"},
     {"GBN_INTERP": "gm"}, {"GBN_INTERP": "db"}, {"GBN_INTERP": "wc"},
     {"GBN_INTERP": "twc"}, {"GBN_INTERP": "tile"},
     {"GBN_INTERP_CG": "2"}, {"GBN_INTERP_CG": "4"},
@@ -78,7 +79,8 @@ def test_variant_matches_oracle(gpu_pkg, monkeypatch, env, dim, sense):
     assert rel_l2(op.data_consistency(x, y), ref.dc(x, y)) < TOL
 
 
-@pytest.mark.parametrize("env", [{}, {"GBN_SPREAD_CG": "8"}, {"GBN_QUAD_MINB": "3"}], ids=_ids)
+@pytest.mark.parametrize("env", [{}, {"GBN_SPREAD_CG": "8"}, {"GBN_QUAD_MINB": "4"},
+                                 {"GBN_SPREAD": "mma"}], ids=_ids)
 @pytest.mark.parametrize("C", [8, 9, 17])
 def test_quadrant_spreader_coil_groups(gpu_pkg, monkeypatch, env, C):
     """The 3D quadrant spreader with 8 coils per pass or 3 CTAs per SM, on
