@@ -32,20 +32,22 @@ constexpr int kMmaRound = 256;  // samples staged at a time
 constexpr int kMmaCG = 4;       // coils per pass
 
 __host__ __device__ constexpr size_t mma_spread_smem_bytes() {
-  return (size_t)kMmaRound * sizeof(int)                 // headers
-         + (size_t)kMmaRound * 24 * sizeof(float)        // wx, wy, wz (8 each)
+  return (size_t)2 * 16 * 32 * sizeof(uint2)             // B fragments, hi and lo
+         + (size_t)kMmaRound * 49 * sizeof(uint32_t)     // x-y weight products, bf16 hi | lo
+         + (size_t)kMmaRound * 8 * sizeof(float)         // wz
          + (size_t)kMmaCG * kMmaRound * sizeof(float2)   // strengths
-         + (size_t)2 * 16 * 32 * sizeof(uint2)           // B fragments, hi and lo
+         + (size_t)kMmaRound * sizeof(int)               // headers
          + (size_t)kStreamChunk * sizeof(short);         // chunk indices in z order
 }
 
-__device__ __forceinline__ void bf16x3_split(float v0, float v1, uint32_t& hi, uint32_t& lo) {
-  // hi packs bf16(v1):bf16(v0) (v0 in the low half, the lower k index of a
-  // fragment register); lo packs the bf16 rounding of the residuals
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(v1), "f"(v0));
-  const float h0 = __uint_as_float(hi << 16);
-  const float h1 = __uint_as_float(hi & 0xffff0000u);
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(v1 - h1), "f"(v0 - h0));
+// bf16 high part of v and bf16 rounding of the residual, packed hi | lo << 16
+__device__ __forceinline__ uint32_t bf16_hilo(float v) {
+  uint32_t h;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(0.f), "f"(v));  // low half = bf16(v)
+  const float r = v - __uint_as_float(h << 16);
+  uint32_t l;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(l) : "f"(r), "f"(0.f));  // high half = bf16(r)
+  return (h & 0xffffu) | (l & 0xffff0000u);
 }
 
 __device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
@@ -61,16 +63,17 @@ __global__ void __launch_bounds__(kMmaThreads, 2) spread_mma3d_kernel(SpreadArgs
   static_assert(W == 7, "the tensor-core spreader is written for w = 7");
   constexpr int CG = kMmaCG;
   extern __shared__ __align__(16) unsigned char s_raw[];
-  uint2* s_bh = reinterpret_cast<uint2*>(s_raw);            // [16 slots][32 lanes]
+  uint2* s_bh = reinterpret_cast<uint2*>(s_raw);                // [16 slots][32 lanes]
   uint2* s_bl = s_bh + 16 * 32;
-  float* s_wx = reinterpret_cast<float*>(s_bl + 16 * 32);   // [kMmaRound][8]
-  float* s_wy = s_wx + kMmaRound * 8;
-  float* s_wz = s_wy + kMmaRound * 8;
+  uint32_t* s_p = reinterpret_cast<uint32_t*>(s_bl + 16 * 32);  // [kMmaRound][49]
+  float* s_wz = reinterpret_cast<float*>(s_p + kMmaRound * 49);   // [kMmaRound][8]
   float2* s_c = reinterpret_cast<float2*>(s_wz + kMmaRound * 8);  // [CG][kMmaRound]
   // per sample: x, y footprint origins in the quadrant (bits 0-3, 4-7), first
-  // z cell minus (cell - 3) (bit 8), z cell (bits 12-31)
+  // footprint cell along z minus (cell - 3) (bit 8), z cell (bits 12-31)
   int* s_hd = reinterpret_cast<int*>(s_c + CG * kMmaRound);
   short* s_list = reinterpret_cast<short*>(s_hd + kMmaRound);
+  unsigned short* s_bh16 = reinterpret_cast<unsigned short*>(s_bh);
+  unsigned short* s_bl16 = reinterpret_cast<unsigned short*>(s_bl);
   __shared__ int s_wsum[kMmaThreads / 32];
 
   const Geom& g = a.g;
@@ -125,21 +128,23 @@ __global__ void __launch_bounds__(kMmaThreads, 2) spread_mma3d_kernel(SpreadArgs
                         : -1;
   }
 
+  // geometry of a round: header, the 7 x 7 products wx wy (bf16 hi | lo),
+  // the z weights
   auto stage_geometry = [&](int r0, int nr) {
     for (int t = threadIdx.x; t < nr; t += blockDim.x) {
       const int pos = p0 + s_list[r0 + t];
-      float wt[W];
-      const int a0 = weights_rt<W>(a.s.u[0][pos], g, wt) - o0;  // 0 .. 4
-#pragma unroll
-      for (int k = 0; k < 8; ++k) s_wx[t * 8 + k] = k < W ? wt[k] : 0.f;
-      const int a1 = weights_rt<W>(a.s.u[1][pos], g, wt) - o1;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) s_wy[t * 8 + k] = k < W ? wt[k] : 0.f;
+      float wx[W], wy[W], wz[W];
+      const int a0 = weights_rt<W>(a.s.u[0][pos], g, wx) - o0;  // 0 .. 4
+      const int a1 = weights_rt<W>(a.s.u[1][pos], g, wy) - o1;
       const float u2 = a.s.u[2][pos];
       const int cell = cell_of(u2, nf2);
-      const int off = weights_rt<W>(u2, g, wt) - (cell - hw);  // 0 or 1
+      const int off = weights_rt<W>(u2, g, wz) - (cell - hw);  // 0 or 1
 #pragma unroll
-      for (int k = 0; k < 8; ++k) s_wz[t * 8 + k] = k < W ? wt[k] : 0.f;
+      for (int i = 0; i < W; ++i)
+#pragma unroll
+        for (int k = 0; k < W; ++k) s_p[t * 49 + i * W + k] = bf16_hilo(wx[i] * wy[k]);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) s_wz[t * 8 + k] = k < W ? wz[k] : 0.f;
       s_hd[t] = a0 | (a1 << 4) | (off << 8) | (cell << 12);
     }
   };
@@ -194,7 +199,8 @@ __global__ void __launch_bounds__(kMmaThreads, 2) spread_mma3d_kernel(SpreadArgs
       __syncthreads();
       int s = 0;
       while (s < nr) {
-        // block: up to 16 samples within 8 cells of the first one (uniform)
+        // block: up to 16 samples in cells within 8 of the first one's, so
+        // that every footprint lies in [cell0 - 3, cell0 + 13) (uniform)
         const int cell0 = s_hd[s] >> 12;
         int n = 1;
         while (n < 16 && s + n < nr && (s_hd[s + n] >> 12) <= cell0 + 8) ++n;
@@ -208,71 +214,83 @@ __global__ void __launch_bounds__(kMmaThreads, 2) spread_mma3d_kernel(SpreadArgs
         have = true;
         zb = zn;
         __syncthreads();  // the previous block's B fragments are consumed
-        // B fragments: entry (slot j, lane L) holds samples 2t', 2t'+1,
-        // 2t'+8, 2t'+9 of column n = g' = (coil, re/im)
-        for (int e = threadIdx.x; e < 16 * 32; e += blockDim.x) {
-          const int j = e >> 5, L = e & 31;
-          const int gg = L >> 2, tt = L & 3;
-          const int cc = gg >> 1, ri = gg & 1;
-          const int z = zb + ((j - zb) & 15);
-          float v[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int k = 2 * tt + (q & 1) + 8 * (q >> 1);
-            float val = 0.f;
-            if (k < n) {
-              const int hd = s_hd[s + k];
-              const int dz = z - ((hd >> 12) - hw + ((hd >> 8) & 1));
-              if ((unsigned)dz < (unsigned)W) {
-                const float2 c = s_c[cc * kMmaRound + s + k];
-                val = s_wz[(s + k) * 8 + dz] * (ri ? c.y : c.x);
-              }
-            }
-            v[q] = val;
+        {
+          // B: thread -> (sample k of the block, column n = (coil, re/im));
+          // its 16 slots, the footprint's 7 nonzero, into the fragment layout
+          // (entry (slot, lane n * 4 + (k & 7) / 2), word k / 8, half k & 1)
+          const int k = threadIdx.x >> 3, nn = threadIdx.x & 7;
+          const int L = nn * 4 + ((k & 7) >> 1);
+          const int hoff = (k >> 3) * 2 + (k & 1);
+          float cv = 0.f;
+          int dz0 = 0;
+          if (k < n) {
+            const float2 c = s_c[(nn >> 1) * kMmaRound + s + k];
+            cv = (nn & 1) ? c.y : c.x;
+            const int hd = s_hd[s + k];
+            dz0 = (hd >> 12) - hw + ((hd >> 8) & 1) - zb;  // 0 .. 9
           }
-          uint2 h, l;
-          bf16x3_split(v[0], v[1], h.x, l.x);
-          bf16x3_split(v[2], v[3], h.y, l.y);
-          s_bh[e] = h;
-          s_bl[e] = l;
-        }
-        // A fragments: rows of the lane, samples 2 tq, 2 tq + 1, 2 tq + 8, 2 tq + 9
-        float av[4][4];  // [row q][sample slot k]
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const int k = 2 * tq + (kk & 1) + 8 * (kk >> 1);
-          int hd = 0;
-          if (k < n) hd = s_hd[s + k];
-          const int ax = hd & 15, ay = (hd >> 4) & 15;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int dx = rx[q] - ax, dy = ry[q] - ay;
-            float val = 0.f;
-            if (k < n && (unsigned)dx < (unsigned)W && (unsigned)dy < (unsigned)W)
-              val = s_wx[(s + k) * 8 + dx] * s_wy[(s + k) * 8 + dy];
-            av[q][kk] = val;
+          for (int j = 0; j < 16; ++j) {
+            const int dz = ((j - zb - dz0) & 15);  // footprint offset of slot j
+            const bool on = k < n && dz < W;
+            const float v = on ? s_wz[on ? (s + k) * 8 + dz : 0] * cv : 0.f;
+            const uint32_t hl = bf16_hilo(v);
+            s_bh16[(j * 32 + L) * 4 + hoff] = (unsigned short)(hl & 0xffffu);
+            s_bl16[(j * 32 + L) * 4 + hoff] = (unsigned short)(hl >> 16);
           }
         }
+        // A fragments from the product table: rows of the lane, samples
+        // 2 tq, 2 tq + 1 (word 0) and 2 tq + 8, 2 tq + 9 (word 1)
         uint32_t ah[2][4], al[2][4];
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-          // a0: (row g, k 2t..2t+1), a1: (row g+8, k 2t..), a2: (row g, k 2t+8..), a3: (row g+8, k 2t+8..)
-          bf16x3_split(av[2 * mt][0], av[2 * mt][1], ah[mt][0], al[mt][0]);
-          bf16x3_split(av[2 * mt + 1][0], av[2 * mt + 1][1], ah[mt][1], al[mt][1]);
-          bf16x3_split(av[2 * mt][2], av[2 * mt][3], ah[mt][2], al[mt][2]);
-          bf16x3_split(av[2 * mt + 1][2], av[2 * mt + 1][3], ah[mt][3], al[mt][3]);
+        for (int kp = 0; kp < 2; ++kp) {
+          const int k0 = 2 * tq + 8 * kp;
+          uint32_t pv[2][4];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int k = k0 + e;
+            const int hd = k < n ? s_hd[s + k] : (15 | (15 << 4));
+            const int ax = hd & 15, ay = (hd >> 4) & 15;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int dx = rx[q] - ax, dy = ry[q] - ay;
+              const bool on = (unsigned)dx < (unsigned)W && (unsigned)dy < (unsigned)W;
+              // the index stays inside the table when the entry is off
+              const uint32_t pe = s_p[on ? (s + k) * 49 + dx * W + dy : 0];
+              pv[e][q] = on ? pe : 0u;
+            }
+          }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              // register 2 kp + h of m-tile mt: row (mt, h), samples k0, k0 + 1
+              const uint32_t x0 = pv[0][2 * mt + h], x1 = pv[1][2 * mt + h];
+              ah[mt][2 * kp + h] = __byte_perm(x0, x1, 0x5410);
+              al[mt][2 * kp + h] = __byte_perm(x0, x1, 0x7632);
+            }
         }
         __syncthreads();  // B fragments written
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const uint2 bh = s_bh[j * 32 + lane];
-          const uint2 bl = s_bl[j * 32 + lane];
+        for (int j0 = 0; j0 < 16; j0 += 4) {
+          uint2 bh[4], bl[4];
 #pragma unroll
-          for (int mt = 0; mt < 2; ++mt) {
-            mma_16816(d[mt][j], al[mt], bh.x, bh.y);
-            mma_16816(d[mt][j], ah[mt], bl.x, bl.y);
-            mma_16816(d[mt][j], ah[mt], bh.x, bh.y);
+          for (int jj = 0; jj < 4; ++jj) {
+            bh[jj] = s_bh[(j0 + jj) * 32 + lane];
+            bl[jj] = s_bl[(j0 + jj) * 32 + lane];
           }
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) mma_16816(d[mt][j0 + jj], al[mt], bh[jj].x, bh[jj].y);
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) mma_16816(d[mt][j0 + jj], ah[mt], bl[jj].x, bl[jj].y);
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) mma_16816(d[mt][j0 + jj], ah[mt], bh[jj].x, bh[jj].y);
         }
         s += n;
       }

@@ -13,7 +13,8 @@ reference's steps one by one with its own functions (``_crop_or_pad``,
 ``_unfold_blocks``, ``fft`` / ``ifft`` of ``extras/cartesian.py``,
 ``power_method`` of ``operators/base.py``, ``_extract_kspace_center`` and an
 ``MRInumpy`` LSQR for the non-Cartesian front end of ``espirit``,
-smaps.py:315-364) and apply the final mask per voxel, the broadcast-correct
+smaps.py:315-364, run in the backend's precision: float32 samples and
+complex64 k-space) and apply the final mask per voxel, the broadcast-correct
 form that the reference's ``decim > 1`` branch uses.  Stored per case: the
 inputs, the maps before the mask, the eigenvalue per voxel and the masked
 maps.  Both the 2D k-space FFT of ``espirit`` and the kernel iFFTs use the
@@ -125,15 +126,19 @@ def main(ref_src):
     y = MRInumpy(traj, shape, n_coils=C, smaps=s).op(img)
     y = y + 0.001 * (rng.standard_normal(y.shape) + 1j * rng.standard_normal(y.shape))
     cw, kw = 16, 5
+    # the front end in the backend's precision (float32 samples, complex64
+    # data): the reference's LSQR itself moves by 5e-3 between complex64 and
+    # complex128 on this system after 10 iterations
+    y = y.astype(np.complex64)
     k_space, samples, _ = _extract_kspace_center(
-        kspace_data=y, kspace_loc=traj, threshold=tuple(float(v) for v in cw / np.asarray(shape)),
-        density=None, window_fun="rect")
+        kspace_data=y, kspace_loc=traj.astype(np.float32),
+        threshold=tuple(float(v) for v in cw / np.asarray(shape)), density=None, window_fun="rect")
     nufft = MRInumpy(samples, shape, n_coils=k_space.shape[-2])
     nufft.squeeze_dims = True
     img_c = nufft.pinv_solver(k_space, max_iter=10)
     central = fft(img_c)
     sm, eig, masked, nk, margin = espirit_steps(central.astype(np.complex64), shape, cw, kw, 0.02, 0.95)
-    out["radial__samples"] = traj
+    out["radial__samples"] = traj.astype(np.float32)
     out["radial__kspace"] = y
     out["radial__shape"] = np.array(shape)
     out["radial__calib_width"] = np.array(cw)

@@ -88,8 +88,9 @@ def test_espirit_non_cartesian_matches_reference(gpu_pkg):
                   g[f"{name}__kspace"].astype(np.complex64), calib_width=cw, kernel_width=kw)
     e_ref = g[f"{name}__eig"]
     sure = np.abs(e_ref - 0.95) > 1e-3
-    # LSQR in float32 against FP64 feeds the eigen-problem: 1e-3
-    assert rel_l2(out[:, sure], g[f"{name}__masked"][:, sure]) < 1e-3
+    # the fixture's front end runs the reference's LSQR in complex64, as this
+    # backend does (in FP64 it moves by 5e-3 on this system)
+    assert rel_l2(out[:, sure], g[f"{name}__masked"][:, sure]) < 1e-4
 
 
 def test_operator_compute_smaps_espirit(gpu_pkg):
