@@ -1215,6 +1215,41 @@ spread_stream3d_kernel(SpreadArgs a) {
   }
 }
 
+// The same for window accumulators held as (re, im) pairs.
+template <int K, int CG>
+__device__ __forceinline__ void stream_flush2(float2 (&acc)[CG][8], bool own, float2* fb, int z,
+                                              int nf2, int G, int nc) {
+  if (own) {
+    float2* dst = fb + wrap_near(z, nf2);
+#pragma unroll
+    for (int cc = 0; cc < CG; ++cc) {
+      if (cc < nc && (acc[cc][K].x != 0.f || acc[cc][K].y != 0.f)) atomicAdd(dst, acc[cc][K]);
+      dst += G;
+    }
+  }
+#pragma unroll
+  for (int cc = 0; cc < CG; ++cc) acc[cc][K] = make_float2(0.f, 0.f);
+}
+
+template <int CG>
+__device__ __forceinline__ void stream_flush_mask2(unsigned mask, int zb, float2 (&acc)[CG][8],
+                                                   bool own, float2* fb, int nf2, int G, int nc) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (mask & (1u << k)) {
+      const int z = zb + ((k - zb) & 7);
+      if (k == 0) stream_flush2<0, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 1) stream_flush2<1, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 2) stream_flush2<2, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 3) stream_flush2<3, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 4) stream_flush2<4, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 5) stream_flush2<5, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 6) stream_flush2<6, CG>(acc, own, fb, z, nf2, G, nc);
+      if (k == 7) stream_flush2<7, CG>(acc, own, fb, z, nf2, G, nc);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Spreading, 3D quadrant-streaming kernel (8 x 8 bins, widths w <= 7).
 //
@@ -1237,7 +1272,9 @@ __host__ __device__ constexpr size_t quad_smem_bytes(int cg) {
          (size_t)cg * kQuadRound * sizeof(float2) + (size_t)kStreamBatch * sizeof(short);
 }
 
-template <int W, int CG, int MINB>
+// PACKED: the window accumulators are (re, im) pairs updated by two-wide
+// FP32 fused multiply-adds (one instruction per cell and coil).
+template <int W, int CG, int MINB, bool PACKED = false>
 __global__ void __launch_bounds__(kQuadThreads, MINB)
 spread_quad3d_kernel(SpreadArgs a) {
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -1333,13 +1370,21 @@ spread_quad3d_kernel(SpreadArgs a) {
   const unsigned mybit = 1u << (24 + warp);
   for (int c0 = 0; c0 < a.ntr; c0 += CG) {
     const int nc = imin(CG, a.ntr - c0);
-    float ar[CG][8], ai[CG][8];
+    float ar[PACKED ? 1 : CG][8], ai[PACKED ? 1 : CG][8];
+    float2 acc[PACKED ? CG : 1][8];
 #pragma unroll
-    for (int cc = 0; cc < CG; ++cc)
+    for (int k = 0; k < 8; ++k) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+      for (int cc = 0; cc < (PACKED ? 1 : CG); ++cc) ar[cc][k] = ai[cc][k] = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < (PACKED ? CG : 1); ++cc) acc[cc][k] = make_float2(0.f, 0.f);
+    }
     float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
     int zb = 0;
+    auto flush = [&](unsigned mask) {
+      if constexpr (PACKED) stream_flush_mask2<CG>(mask, zb, acc, own, fb, nf2, G, nc);
+      else stream_flush_mask<CG>(mask, zb, ar, ai, own, fb, nf2, G, nc);
+    };
     for (int r0 = 0; r0 < n_own; r0 += kQuadRound) {
       const int nr = imin(kQuadRound, n_own - r0);
       if (!once) stage_geometry(r0, nr);
@@ -1362,7 +1407,7 @@ spread_quad3d_kernel(SpreadArgs a) {
         if (zs != zb) {  // the same for every thread: flush the cells that leave the window
           const int steps = imin(zs - zb, 8);
           const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
-          stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf2, G, nc);
+          flush(((m << r) | (m >> (8u - r))) & 0xffu);
           zb = zs;
         }
         if (hd & mybit) {  // warp-uniform
@@ -1376,11 +1421,18 @@ spread_quad3d_kernel(SpreadArgs a) {
 #pragma unroll
             for (int cc = 0; cc < CG; ++cc) {
               const float2 c = s_c[cc * kQuadRound + s];
-              const float vr = kw * c.x, vi = kw * c.y;
+              if constexpr (PACKED) {
+                const float2 v = __fmul2_rn(c, make_float2(kw, kw));
 #pragma unroll
-              for (int k = 0; k < 8; ++k) {
-                ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
-                ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
+                for (int k = 0; k < 8; ++k)
+                  acc[cc][k] = __ffma2_rn(v, make_float2(wz[k], wz[k]), acc[cc][k]);
+              } else {
+                const float vr = kw * c.x, vi = kw * c.y;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                  ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
+                  ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
+                }
               }
             }
           }
@@ -1388,7 +1440,7 @@ spread_quad3d_kernel(SpreadArgs a) {
       }
       __syncthreads();  // staged strengths (and geometry) are replaced next
     }
-    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf2, G, nc);
+    flush(0xffu);
   }
 }
 
@@ -1972,11 +2024,11 @@ cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int W, int CG, int MINB = 4>
+template <int W, int CG, int MINB = 4, bool PACKED = false>
 cudaError_t launch_spread_quad_t(const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return cudaSuccess;
   const size_t smem = quad_smem_bytes(CG);
-  auto k = spread_quad3d_kernel<W, CG, MINB>;
+  auto k = spread_quad3d_kernel<W, CG, MINB, PACKED>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<(unsigned)(4 * (int64_t)a.s.nsub), kQuadThreads, smem, st>>>(a);
@@ -2004,6 +2056,8 @@ inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st
       // cap spills, on the 16-coil 3D kooshball); GBN_QUAD_MINB=4 keeps 4
       // CTAs; GBN_SPREAD_CG=8 runs 8 coils per pass at 2 CTAs per SM (7.50 ms)
       if (a.g.spread_cg == 8 && a.ntr >= 8) return launch_spread_quad_t<7, 8, 2>(a, st);
+      // GBN_QUAD_PACKED=1: (re, im) accumulator pairs with two-wide FMAs
+      if (cg == 4 && a.g.quad_packed == 1) return launch_spread_quad_t<7, 4, 3, true>(a, st);
       if (cg == 4 && a.g.quad_minb == 4) return launch_spread_quad_t<7, 4, 4>(a, st);
       if (cg == 4) return launch_spread_quad_t<7, 4, 3>(a, st);
       return cg == 2 ? launch_spread_quad_t<7, 2>(a, st) : launch_spread_quad_t<7, 1>(a, st);
