@@ -595,6 +595,7 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
     if (const char* e = std::getenv("GBN_INTERP_CG")) g.interp_cg = std::atoi(e);
     if (const char* e = std::getenv("GBN_SPREAD_CG")) g.spread_cg = std::atoi(e);
     if (const char* e = std::getenv("GBN_QUAD_MINB")) g.quad_minb = std::atoi(e);
+    g.quad_packed = 1;
     if (const char* e = std::getenv("GBN_QUAD_PACKED")) g.quad_packed = std::atoi(e);
     if (const char* e = std::getenv("GBN_INTERP"))
       g.method_interp = std::strcmp(e, "gm") == 0   ? 1

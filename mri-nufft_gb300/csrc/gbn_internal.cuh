@@ -47,7 +47,7 @@ struct Geom {
   int interp_threads; // CTA size of the tile interp kernel (0: 128)
   int spread_cg;      // coils per pass of the streaming spreader (0: automatic)
   int quad_minb;      // resident CTAs per SM of the 4-coil quadrant spreader (0: 3)
-  int quad_packed;    // 1: the quadrant spreader's accumulators as (re, im) pairs
+  int quad_packed;    // 0: scalar accumulators in the quadrant spreader (default 1: (re, im) pairs)
 };
 
 // Work table of one sorted trajectory.

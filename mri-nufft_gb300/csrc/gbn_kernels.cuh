@@ -207,29 +207,32 @@ __device__ __forceinline__ void load_tile_async(float2* tile, const float2* __re
 // ---------------------------------------------------------------------------
 // Interpolation
 // ---------------------------------------------------------------------------
-// Footprint sum of one sample over the staged tiles of CG transforms.
+// Footprint sum of one sample over the staged tiles of CG transforms.  The
+// (re, im) sums are carried as pairs by two-wide FMAs.
 template <int DIM, int W, int CG>
 __device__ __forceinline__ void interp_footprint(const float2* cur, const Geom& g, int T,
                                                  const float* w0, const float* w1, const float* w2,
                                                  int l0, int l1, int l2, float* ar, float* ai) {
+  constexpr int WM = WidthTraits<W>::WM;
   const int WL = W > 0 ? W : g.w;
+  float2 acc[CG];
 GBN_UNROLL
-  for (int cc = 0; cc < CG; ++cc) { ar[cc] = 0.f; ai[cc] = 0.f; }
+  for (int cc = 0; cc < CG; ++cc) acc[cc] = make_float2(0.f, 0.f);
+  const float* wl = DIM == 2 ? w1 : w2;  // weights of the last axis
+  float2 wp[WM];
+GBN_UNROLL
+  for (int t = 0; t < WM; ++t) wp[t] = make_float2(wl[t], wl[t]);
   if (DIM == 2) {
 GBN_UNROLL
     for (int t0 = 0; t0 < WL; ++t0) {
       const float2* row = cur + (l0 + t0) * g.pd[1] + l1;
+      const float2 wx = make_float2(w0[t0], w0[t0]);
 GBN_UNROLL
       for (int cc = 0; cc < CG; ++cc) {
-        float sr = 0.f, si = 0.f;
+        float2 sv = make_float2(0.f, 0.f);
 GBN_UNROLL
-        for (int t1 = 0; t1 < WL; ++t1) {
-          float2 v = row[cc * T + t1];
-          sr = fmaf(w1[t1], v.x, sr);
-          si = fmaf(w1[t1], v.y, si);
-        }
-        ar[cc] = fmaf(w0[t0], sr, ar[cc]);
-        ai[cc] = fmaf(w0[t0], si, ai[cc]);
+        for (int t1 = 0; t1 < WL; ++t1) sv = __ffma2_rn(wp[t1], row[cc * T + t1], sv);
+        acc[cc] = __ffma2_rn(wx, sv, acc[cc]);
       }
     }
   } else {
@@ -238,21 +241,22 @@ GBN_UNROLL
 GBN_UNROLL
       for (int t1 = 0; t1 < WL; ++t1) {
         const float wy = w0[t0] * w1[t1];
+        const float2 wyp = make_float2(wy, wy);
         const float2* row = cur + ((l0 + t0) * g.pd[1] + (l1 + t1)) * g.pd[2] + l2;
 GBN_UNROLL
         for (int cc = 0; cc < CG; ++cc) {
-          float sr = 0.f, si = 0.f;
+          float2 sv = make_float2(0.f, 0.f);
 GBN_UNROLL
-          for (int t2 = 0; t2 < WL; ++t2) {
-            float2 v = row[cc * T + t2];
-            sr = fmaf(w2[t2], v.x, sr);
-            si = fmaf(w2[t2], v.y, si);
-          }
-          ar[cc] = fmaf(wy, sr, ar[cc]);
-          ai[cc] = fmaf(wy, si, ai[cc]);
+          for (int t2 = 0; t2 < WL; ++t2) sv = __ffma2_rn(wp[t2], row[cc * T + t2], sv);
+          acc[cc] = __ffma2_rn(wyp, sv, acc[cc]);
         }
       }
     }
+  }
+GBN_UNROLL
+  for (int cc = 0; cc < CG; ++cc) {
+    ar[cc] = acc[cc].x;
+    ai[cc] = acc[cc].y;
   }
 }
 
@@ -722,31 +726,25 @@ __device__ __forceinline__ void interp_wc_body(const InterpArgs& a, const int64_
     const float2* base = a.fine + (int64_t)c * g.G;
     float ar = 0.f, ai = 0.f;
     if (act) {
+      // (re, im) sums carried as pairs by two-wide FMAs
+      float2 acc = make_float2(0.f, 0.f);
       if (DIM == 2) {
 #pragma unroll
-        for (int t0 = 0; t0 < W; ++t0) {
-          const float2 v = __ldg(base + rb[t0] + ml);
-          ar = fmaf(w0[t0], v.x, ar);
-          ai = fmaf(w0[t0], v.y, ai);
-        }
-        ar *= wl;
-        ai *= wl;
+        for (int t0 = 0; t0 < W; ++t0)
+          acc = __ffma2_rn(make_float2(w0[t0], w0[t0]), __ldg(base + rb[t0] + ml), acc);
       } else {
 #pragma unroll
         for (int t0 = 0; t0 < W; ++t0) {
-          float sr = 0.f, si = 0.f;
+          float2 sv = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int t1 = 0; t1 < W; ++t1) {
-            const float2 v = __ldg(base + (int64_t)(rb[t0] + m1[t1]) * g.nf[2] + ml);
-            sr = fmaf(w1[t1], v.x, sr);
-            si = fmaf(w1[t1], v.y, si);
-          }
-          ar = fmaf(w0[t0], sr, ar);
-          ai = fmaf(w0[t0], si, ai);
+          for (int t1 = 0; t1 < W; ++t1)
+            sv = __ffma2_rn(make_float2(w1[t1], w1[t1]),
+                            __ldg(base + (int64_t)(rb[t0] + m1[t1]) * g.nf[2] + ml), sv);
+          acc = __ffma2_rn(make_float2(w0[t0], w0[t0]), sv, acc);
         }
-        ar *= wl;
-        ai *= wl;
       }
+      ar = acc.x * wl;
+      ai = acc.y * wl;
     }
 #pragma unroll
     for (int o = 1; o < 8; o <<= 1) {
@@ -1535,11 +1533,11 @@ spread_stream2d_kernel(SpreadArgs a) {
     const int c0 = cp + warp * CG;
     const int nc = imin(CG, a.ntr - c0);
     if (nc <= 0 || cnt == 0) continue;
-    float ar[CG][8], ai[CG][8];
+    float2 acc[CG][8];  // (re, im) pairs, two-wide FMAs
 #pragma unroll
     for (int cc = 0; cc < CG; ++cc)
 #pragma unroll
-      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+      for (int k = 0; k < 8; ++k) acc[cc][k] = make_float2(0.f, 0.f);
     float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
     const float2* sc = s_c + warp * CG * kStream2Batch;
     int zb = (int)(s_hd[0] & 0x3fffu) - 8;
@@ -1550,7 +1548,7 @@ spread_stream2d_kernel(SpreadArgs a) {
       if (zs != zb) {  // the same for every lane: flush the cells that leave the window
         const int steps = imin(zs - zb, 8);
         const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
-        stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+        stream_flush_mask2<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, acc, own, fb, nf1, G, nc);
         zb = zs;
       }
       const unsigned r0 = (unsigned)(lane - (int)((hd >> 14) & 63u));
@@ -1561,17 +1559,13 @@ spread_stream2d_kernel(SpreadArgs a) {
         const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
 #pragma unroll
         for (int cc = 0; cc < CG; ++cc) {
-          const float2 c = sc[cc * kStream2Batch + s];
-          const float vr = kw * c.x, vi = kw * c.y;
+          const float2 v = __fmul2_rn(sc[cc * kStream2Batch + s], make_float2(kw, kw));
 #pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
-            ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
-          }
+          for (int k = 0; k < 8; ++k) acc[cc][k] = __ffma2_rn(v, make_float2(wz[k], wz[k]), acc[cc][k]);
         }
       }
     }
-    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+    stream_flush_mask2<CG>(0xffu, zb, acc, own, fb, nf1, G, nc);
   }
 }
 
@@ -1693,11 +1687,11 @@ spread_half2d_kernel(SpreadArgs a) {
     const int c0 = cp + warp * CG;
     const int nc = imin(CG, a.ntr - c0);
     if (nc <= 0 || cnt == 0) continue;
-    float ar[CG][8], ai[CG][8];
+    float2 acc[CG][8];  // (re, im) pairs, two-wide FMAs
 #pragma unroll
     for (int cc = 0; cc < CG; ++cc)
 #pragma unroll
-      for (int k = 0; k < 8; ++k) ar[cc][k] = ai[cc][k] = 0.f;
+      for (int k = 0; k < 8; ++k) acc[cc][k] = make_float2(0.f, 0.f);
     float2* const fb = a.fine + (int64_t)c0 * g.G + rowbase;
     const float2* sc = s_c + warp * CG * kStream2Batch;
     int zb = nmine > 0 ? (int)(s_hd[lst[0]] & 0x3fffu) - 8 : 0;
@@ -1710,7 +1704,7 @@ spread_half2d_kernel(SpreadArgs a) {
         if (zs != zb) {  // the same for every lane of the half
           const int steps = imin(zs - zb, 8);
           const unsigned m = (1u << steps) - 1u, r = (unsigned)zb & 7u;
-          stream_flush_mask<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+          stream_flush_mask2<CG>(((m << r) | (m >> (8u - r))) & 0xffu, zb, acc, own, fb, nf1, G, nc);
           zb = zs;
         }
         const unsigned r0 = (unsigned)(row - (int)((hd >> 14) & 63u));
@@ -1721,18 +1715,14 @@ spread_half2d_kernel(SpreadArgs a) {
           const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
 #pragma unroll
           for (int cc = 0; cc < CG; ++cc) {
-            const float2 c = sc[cc * kStream2Batch + s];
-            const float vr = kw * c.x, vi = kw * c.y;
+            const float2 v = __fmul2_rn(sc[cc * kStream2Batch + s], make_float2(kw, kw));
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              ar[cc][k] = fmaf(vr, wz[k], ar[cc][k]);
-              ai[cc][k] = fmaf(vi, wz[k], ai[cc][k]);
-            }
+            for (int k = 0; k < 8; ++k) acc[cc][k] = __ffma2_rn(v, make_float2(wz[k], wz[k]), acc[cc][k]);
           }
         }
       }
     }
-    stream_flush_mask<CG>(0xffu, zb, ar, ai, own, fb, nf1, G, nc);
+    stream_flush_mask2<CG>(0xffu, zb, acc, own, fb, nf1, G, nc);
   }
 }
 
@@ -2056,8 +2046,10 @@ inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st
       // cap spills, on the 16-coil 3D kooshball); GBN_QUAD_MINB=4 keeps 4
       // CTAs; GBN_SPREAD_CG=8 runs 8 coils per pass at 2 CTAs per SM (7.50 ms)
       if (a.g.spread_cg == 8 && a.ntr >= 8) return launch_spread_quad_t<7, 8, 2>(a, st);
-      // GBN_QUAD_PACKED=1: (re, im) accumulator pairs with two-wide FMAs
-      if (cg == 4 && a.g.quad_packed == 1) return launch_spread_quad_t<7, 4, 3, true>(a, st);
+      // (re, im) accumulator pairs with two-wide FMAs (measured 6.11 against
+      // 7.09 ms on the 16-coil 3D kooshball); GBN_QUAD_PACKED=0 keeps scalar
+      // accumulators
+      if (cg == 4 && a.g.quad_packed != 0) return launch_spread_quad_t<7, 4, 3, true>(a, st);
       if (cg == 4 && a.g.quad_minb == 4) return launch_spread_quad_t<7, 4, 4>(a, st);
       if (cg == 4) return launch_spread_quad_t<7, 4, 3>(a, st);
       return cg == 2 ? launch_spread_quad_t<7, 2>(a, st) : launch_spread_quad_t<7, 1>(a, st);

@@ -29,7 +29,7 @@ VARIANTS = [
     {},
     {"GBN_SPREAD": "gm"}, {"GBN_SPREAD": "wc"}, {"GBN_SPREAD": "stream"},
     {"GBN_SPREAD": "rows"}, {"GBN_SPREAD": "quad"}, {"GBN_SPREAD": "mma"},
-    {"GBN_QUAD_PACKED": "1"},
+    {"GBN_QUAD_PACKED": "0"},
     {"GBN_INTERP": "gm"}, {"GBN_INTERP": "db"}, {"GBN_INTERP": "wc"},
     {"GBN_INTERP": "twc"}, {"GBN_INTERP": "tile"},
     {"GBN_INTERP_CG": "2"}, {"GBN_INTERP_CG": "4"},
@@ -81,7 +81,7 @@ def test_variant_matches_oracle(gpu_pkg, monkeypatch, env, dim, sense):
 
 
 @pytest.mark.parametrize("env", [{}, {"GBN_SPREAD_CG": "8"}, {"GBN_QUAD_MINB": "4"},
-                                 {"GBN_QUAD_PACKED": "1"}, {"GBN_SPREAD": "mma"}], ids=_ids)
+                                 {"GBN_QUAD_PACKED": "0"}, {"GBN_SPREAD": "mma"}], ids=_ids)
 @pytest.mark.parametrize("C", [8, 9, 17])
 def test_quadrant_spreader_coil_groups(gpu_pkg, monkeypatch, env, C):
     """The 3D quadrant spreader with 8 coils per pass or 3 CTAs per SM, on
