@@ -48,6 +48,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-density", action="store_true",
+                   help="skip the pipe density (and its timing): a small case whose first "
+                        "launches are the op / adj kernels, for profiler captures")
     p.add_argument("--spokes", type=int, default=4096)
     p.add_argument("--samples", type=int, default=512)
     p.add_argument("--coils", type=int, default=16)
@@ -340,15 +343,17 @@ def run_gb300(args):
 
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    dens = pkg.MRIGB300.pipe(torch.from_numpy(traj).to(dev), shape, max_iter=10, device=local)
+    dens = None
+    if not args.no_density:
+        dens = pkg.MRIGB300.pipe(torch.from_numpy(traj).to(dev), shape, max_iter=10, device=local)
     torch.cuda.synchronize()
     pipe_cold_ms = (time.perf_counter() - t0) * 1e3
 
-    op = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps, density=dens, squeeze_dims=False,
-                      device=local)
+    op = pkg.MRIGB300(traj, shape, n_coils=C, smaps=smaps,
+                      density=False if dens is None else dens, squeeze_dims=False, device=local)
     plan = op.plan
     img_d = torch.from_numpy(img).to(dev).reshape(1, *shape)
-    pipe = measure_pipe(pkg, op._samples_d, shape, local)
+    pipe = None if args.no_density else measure_pipe(pkg, op._samples_d, shape, local)
 
     def step():
         y = op._op_device(img_d)
@@ -479,12 +484,13 @@ def run_gb300(args):
                 "call": "op.adj_op(op.op(x)) on a device copy of a pinned host image, result "
                         "copied back to pinned host memory; CUDA events"},
         "e2e_numpy": e2e_np,
-        "pipe": dict(pipe, cold_ms=pipe_cold_ms, peak_gbs=peak,
-                     roofline_frac=pipe["spread_achieved_gbs"] / peak),
+        "pipe": None if pipe is None else dict(pipe, cold_ms=pipe_cold_ms, peak_gbs=peak,
+                                               roofline_frac=pipe["spread_achieved_gbs"] / peak),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(traj, shape, img, smaps,
-                                            dens.cpu().numpy() if hasattr(dens, "cpu") else dens, C)
+                                            np.ones(M, np.float32) if dens is None
+                                            else dens.cpu().numpy(), C)
         line["accuracy"] = accuracy_vs_ndft(op, img, traj, shape, smaps=smaps, rows=4096,
                                             vox_per_axis=16)
     if rank == 0:
