@@ -1265,10 +1265,8 @@ __device__ __forceinline__ void stream_flush_mask2(unsigned mask, int zb, float2
 constexpr int kQuadThreads = 128;
 constexpr int kQuadRound = 256;  // samples staged at a time
 
-// packed: the z weights are staged twice each, as (w, w) pairs for the
-// two-wide FMAs
-__host__ __device__ constexpr size_t quad_smem_bytes(int cg, bool packed = false) {
-  return (size_t)kQuadRound * (sizeof(unsigned) + (packed ? 32 : 24) * sizeof(float)) +
+__host__ __device__ constexpr size_t quad_smem_bytes(int cg) {
+  return (size_t)kQuadRound * (sizeof(unsigned) + 24 * sizeof(float)) +
          (size_t)cg * kQuadRound * sizeof(float2) + (size_t)kStreamBatch * sizeof(short);
 }
 
@@ -1279,8 +1277,7 @@ __global__ void __launch_bounds__(kQuadThreads, MINB)
 spread_quad3d_kernel(SpreadArgs a) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   float* s_w2 = reinterpret_cast<float*>(s_raw);           // [kQuadRound][8], slot order
-  constexpr int WZS = PACKED ? 16 : 8;                      // z weights per sample
-  float* s_w0 = s_w2 + kQuadRound * WZS;                    // [kQuadRound][8]
+  float* s_w0 = s_w2 + kQuadRound * 8;                      // [kQuadRound][8]
   float* s_w1 = s_w0 + kQuadRound * 8;                      // [kQuadRound][8]
   float2* s_c = reinterpret_cast<float2*>(s_w1 + kQuadRound * 8);  // [CG][kQuadRound]
   // per sample: window anchor + 8 (bits 0-15), quadrant row offsets a0, a1
@@ -1355,12 +1352,7 @@ spread_quad3d_kernel(SpreadArgs a) {
 #pragma unroll
         for (int kk = 0; kk < WidthTraits<W>::WM; ++kk)
           if (kk == m && kk < w) v = wt[kk];
-        if constexpr (PACKED) {
-          s_w2[t * 16 + 2 * ((zs + k) & 7)] = v;
-          s_w2[t * 16 + 2 * ((zs + k) & 7) + 1] = v;
-        } else {
-          s_w2[t * 8 + ((zs + k) & 7)] = v;
-        }
+        s_w2[t * 8 + ((zs + k) & 7)] = v;
       }
       // warp q's threads own quadrant rows (32 q) / pdq .. (32 q + 31) / pdq along x
       unsigned wm = 0;
@@ -1421,29 +1413,17 @@ spread_quad3d_kernel(SpreadArgs a) {
           const unsigned r1w = (unsigned)(i1 - (int)((hd >> 20) & 15u));
           if (own && r0w < (unsigned)w && r1w < (unsigned)w) {
             const float kw = s_w0[s * 8 + r0w] * s_w1[s * 8 + r1w];
-            float wz[8];
-            float2 wzp[8];
-            if constexpr (PACKED) {
-              const float4* w4 = reinterpret_cast<const float4*>(s_w2 + s * 16);
-#pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                const float4 wq = w4[q];
-                wzp[2 * q] = make_float2(wq.x, wq.y);
-                wzp[2 * q + 1] = make_float2(wq.z, wq.w);
-              }
-            } else {
-              const float4* w4 = reinterpret_cast<const float4*>(s_w2 + s * 8);
-              const float4 wa = w4[0], wb = w4[1];
-              wz[0] = wa.x; wz[1] = wa.y; wz[2] = wa.z; wz[3] = wa.w;
-              wz[4] = wb.x; wz[5] = wb.y; wz[6] = wb.z; wz[7] = wb.w;
-            }
+            const float4* w4 = reinterpret_cast<const float4*>(s_w2 + s * 8);
+            const float4 wa = w4[0], wb = w4[1];
+            const float wz[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
 #pragma unroll
             for (int cc = 0; cc < CG; ++cc) {
               const float2 c = s_c[cc * kQuadRound + s];
               if constexpr (PACKED) {
                 const float2 v = __fmul2_rn(c, make_float2(kw, kw));
 #pragma unroll
-                for (int k = 0; k < 8; ++k) acc[cc][k] = __ffma2_rn(v, wzp[k], acc[cc][k]);
+                for (int k = 0; k < 8; ++k)
+                  acc[cc][k] = __ffma2_rn(v, make_float2(wz[k], wz[k]), acc[cc][k]);
               } else {
                 const float vr = kw * c.x, vi = kw * c.y;
 #pragma unroll
@@ -2037,7 +2017,7 @@ cudaError_t launch_spread_stream_t(const SpreadArgs& a, cudaStream_t st) {
 template <int W, int CG, int MINB = 4, bool PACKED = false>
 cudaError_t launch_spread_quad_t(const SpreadArgs& a, cudaStream_t st) {
   if (a.s.nsub == 0) return cudaSuccess;
-  const size_t smem = quad_smem_bytes(CG, PACKED);
+  const size_t smem = quad_smem_bytes(CG);
   auto k = spread_quad3d_kernel<W, CG, MINB, PACKED>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
