@@ -2045,7 +2045,9 @@ inline cudaError_t dispatch_spread_stream3d(const SpreadArgs& a, cudaStream_t st
       // measured 7.08 against 7.63 ms at 4 CTAs per SM, whose 128-register
       // cap spills, on the 16-coil 3D kooshball); GBN_QUAD_MINB=4 keeps 4
       // CTAs; GBN_SPREAD_CG=8 runs 8 coils per pass at 2 CTAs per SM (7.50 ms)
-      if (a.g.spread_cg == 8 && a.ntr >= 8) return launch_spread_quad_t<7, 8, 2>(a, st);
+      if (a.g.spread_cg == 8 && a.ntr >= 8)
+        return a.g.quad_packed != 0 ? launch_spread_quad_t<7, 8, 2, true>(a, st)
+                                    : launch_spread_quad_t<7, 8, 2>(a, st);
       // (re, im) accumulator pairs with two-wide FMAs (measured 6.11 against
       // 7.09 ms on the 16-coil 3D kooshball); GBN_QUAD_PACKED=0 keeps scalar
       // accumulators
