@@ -316,8 +316,6 @@ class MRIGB300(_Base):
         r"""Forward operator: for every batch b and coil l, :math:`F S_l x_b`."""
         self.check_shape(image=data, ksp=ksp)
         like = _array.interface_of(data)
-        if like.kind == "numpy" and ksp is None and self._host_groups() > 1:
-            return self._safe_squeeze(self._op_host(data))
         ret = self._safe_squeeze(self._op_device(self._img_tensor(data)))
         return self._emit(ret, like, ksp)
 
@@ -325,103 +323,8 @@ class MRIGB300(_Base):
         """Adjoint operator (density compensated when density is set)."""
         self.check_shape(image=img, ksp=coeffs)
         like = _array.interface_of(coeffs)
-        if like.kind == "numpy" and img is None and self._host_groups() > 1:
-            return self._safe_squeeze(self._adj_host(coeffs))
         ret = self._safe_squeeze(self._adj_device(self._ksp_tensor(coeffs)))
         return self._emit(ret, like, img)
-
-    # --------------------------------------------- host arrays, overlapped
-    # Host (numpy) k-space of many coils is large (16 coils x 2.1 M samples
-    # = 268 MB).  For such calls the coils are transformed in groups and the
-    # host <-> device copy of one group (pageable memory: the calling thread
-    # waits for it) runs while the GPU works on the next group.
-    HOST_OVERLAP_BYTES = 32 << 20
-
-    def _host_groups(self):
-        C = self.n_coils
-        if C < 2 or 8 * C * self.n_samples < self.HOST_OVERLAP_BYTES:
-            return 1
-        return min(4, C)
-
-    def _copy_stream(self):
-        if getattr(self, "_copy_st", None) is None:
-            self._copy_st = torch.cuda.Stream(self.device)
-        return self._copy_st
-
-    def _coil_groups(self):
-        C, n = self.n_coils, self._host_groups()
-        step = -(-C // n)
-        return [(c0, min(C, c0 + step)) for c0 in range(0, C, step)]
-
-    def _op_host(self, data):
-        """op of a numpy image: groups of coils, the device-to-host copy of a
-        group's k-space overlapping the next group's transforms."""
-        B, C, M = self.n_batchs, self.n_coils, self.n_samples
-        x = self._img_tensor(data)
-        dev_k = torch.empty((B, C, M), dtype=torch.complex64, device=self.device)
-        out = np.empty((B, C, M), dtype=np.complex64)
-        out_t = torch.from_numpy(out)
-        main = torch.cuda.current_stream(self.device)
-        side = self._copy_stream()
-        work = [(b, c0, c1) for b in range(B) for c0, c1 in self._coil_groups()]
-        events = []
-
-        def launch(b, c0, c1):
-            nc = c1 - c0
-            if self.uses_sense:
-                img, sm = x[b:b + 1], self._smaps[c0:c1]
-            else:
-                img, sm = x[b * C + c0:b * C + c1], None
-            self._plan.op(img, sm, dev_k[b, c0:c1], 1, nc, self.inv_norm_factor, isign=self._isign)
-            ev = torch.cuda.Event()
-            ev.record(main)
-            return ev
-
-        events.append(launch(*work[0]))
-        for i, (b, c0, c1) in enumerate(work):
-            if i + 1 < len(work):
-                events.append(launch(*work[i + 1]))  # queued before this group's copy waits
-            side.wait_event(events[i])
-            with torch.cuda.stream(side):
-                out_t[b, c0:c1].copy_(dev_k[b, c0:c1])
-        side.synchronize()
-        return out
-
-    def _adj_host(self, coeffs):
-        """adj_op of numpy k-space: groups of coils, the host-to-device copy of
-        the next group overlapping this group's adjoint transforms; SENSE
-        images of the groups are summed on the device."""
-        B, C, M = self.n_batchs, self.n_coils, self.n_samples
-        a = np.asarray(coeffs)
-        if a.dtype != np.complex64:
-            a = a.astype(np.complex64)
-        y_t = torch.from_numpy(np.ascontiguousarray(a)).reshape(B, C, M)
-        dev_k = torch.empty((B, C, M), dtype=torch.complex64, device=self.device)
-        sense = self.uses_sense
-        shape = (B, 1, *self.shape) if sense else (B, C, *self.shape)
-        out_d = torch.empty(shape, dtype=torch.complex64, device=self.device)
-        part = torch.empty((1, 1, *self.shape), dtype=torch.complex64, device=self.device) if sense else None
-        main = torch.cuda.current_stream(self.device)
-        side = self._copy_stream()
-        side.wait_stream(main)  # dev_k is allocated on the main stream
-        for b in range(B):
-            for gi, (c0, c1) in enumerate(self._coil_groups()):
-                with torch.cuda.stream(side):
-                    dev_k[b, c0:c1].copy_(y_t[b, c0:c1])  # overlaps the previous group's kernels
-                ev = torch.cuda.Event()
-                ev.record(side)
-                main.wait_event(ev)
-                nc = c1 - c0
-                if sense:
-                    dst = out_d[b:b + 1] if gi == 0 else part
-                    self._plan.adj(dev_k[b:b + 1, c0:c1], self._density, self._smaps[c0:c1], dst, 1, nc,
-                                   self.inv_norm_factor, isign=-self._isign)
-                    if gi > 0:
-                        out_d[b:b + 1] += part
-                else:
-                    self._plan.adj(dev_k[b:b + 1, c0:c1], self._density, None, out_d[b, c0:c1], 1, nc,
-                                   self.inv_norm_factor, isign=-self._isign)
-        return out_d.cpu().numpy()
 
     def _op(self, image, coeffs):
         """Unnormalised type-2 transforms of an (n, *shape) image stack."""
