@@ -436,7 +436,8 @@ def run_gb300(args):
               "steps": nsteps_np,
               "h2d_bytes_per_step": img_np.nbytes + M * C * 8,
               "d2h_bytes_per_step": M * C * 8 + int(np.asarray(out_np).nbytes),
-              "call": "op.adj_op(op.op(numpy image)) -> numpy image; host-timed"}
+              "call": "op.adj_op(op.op(numpy image)) -> numpy image; host-timed; numpy "
+                      "results in page-locked memory, op's k-space copied out per coil group"}
 
     # ---- roofline of the dominant kernel ----
     peaks_path = ROOT / "MEASURED_PEAKS.json"

@@ -7,6 +7,13 @@ DLPack producer) is what comes out, on the same device.  Device arrays
 cross zero-copy through DLPack when they already are contiguous complex64
 on the operator's GPU; host arrays are copied to the device once and the
 result copied back once.
+
+Host (numpy) results are returned in page-locked memory taken from torch's
+caching host allocator (``PINNED_RESULTS``): the device-to-host copy then
+runs at DMA speed, and a numpy result passed back in (``adj_op(op(x))``, the
+iterations of a solver on host arrays) is copied to the device
+asynchronously as a page-locked buffer.  The arrays are ordinary numpy
+arrays; a freed one returns its block to the allocator's cache.
 """
 
 from __future__ import annotations
@@ -15,6 +22,9 @@ from dataclasses import dataclass
 
 import numpy as np
 import torch
+
+# numpy results in page-locked host memory (False: pageable ``Tensor.cpu()``)
+PINNED_RESULTS = True
 
 
 @dataclass
@@ -77,4 +87,9 @@ def from_tensor(t: torch.Tensor, like: Interface):
         return cp.from_dlpack(t)
     if like.kind == "cai":
         return t
+    if PINNED_RESULTS and t.is_cuda:
+        out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        out.copy_(t, non_blocking=True)
+        torch.cuda.current_stream(t.device).synchronize()
+        return out.numpy()
     return t.cpu().numpy()

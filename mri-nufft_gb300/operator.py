@@ -316,6 +316,8 @@ class MRIGB300(_Base):
         r"""Forward operator: for every batch b and coil l, :math:`F S_l x_b`."""
         self.check_shape(image=data, ksp=ksp)
         like = _array.interface_of(data)
+        if like.kind == "numpy" and ksp is None and self._host_groups() > 1:
+            return self._safe_squeeze(self._op_host(data))
         ret = self._safe_squeeze(self._op_device(self._img_tensor(data)))
         return self._emit(ret, like, ksp)
 
@@ -325,6 +327,58 @@ class MRIGB300(_Base):
         like = _array.interface_of(coeffs)
         ret = self._safe_squeeze(self._adj_device(self._ksp_tensor(coeffs)))
         return self._emit(ret, like, img)
+
+    # --------------------------------------------- host arrays, overlapped
+    # Host (numpy) k-space of many coils is large (16 coils x 2.1 M samples
+    # = 268 MB).  op of a numpy image transforms the coils in groups and
+    # copies each group's k-space into the page-locked result on a copy
+    # stream while the GPU works on the next group (3D kooshball, 16 coils:
+    # 7.6 against 8.1 ms per call).  adj_op makes one call over all coils:
+    # its kernels need the k-space before they start, and group calls would
+    # cost more than the copy they hide (2.2 ms per 4-coil group against
+    # 2.0 ms per pass of one call, whose kernels stage each sample's geometry
+    # once for every coil).
+    HOST_OVERLAP_BYTES = 32 << 20
+
+    def _host_groups(self):
+        C = self.n_coils
+        if (not _array.PINNED_RESULTS or C < 2
+                or 8 * C * self.n_samples * self.n_batchs < self.HOST_OVERLAP_BYTES):
+            return 1
+        return min(4, C)
+
+    def _copy_stream(self):
+        if getattr(self, "_copy_st", None) is None:
+            self._copy_st = torch.cuda.Stream(self.device)
+        return self._copy_st
+
+    def _coil_groups(self):
+        C, n = self.n_coils, self._host_groups()
+        step = -(-C // n)
+        return [(c0, min(C, c0 + step)) for c0 in range(0, C, step)]
+
+    def _op_host(self, data):
+        """op of a numpy image: groups of coils, the device-to-host copy of a
+        group's k-space overlapping the next group's transforms."""
+        B, C, M = self.n_batchs, self.n_coils, self.n_samples
+        x = self._img_tensor(data)
+        dev_k = torch.empty((B, C, M), dtype=torch.complex64, device=self.device)
+        out = torch.empty((B, C, M), dtype=torch.complex64, pin_memory=True)
+        main = torch.cuda.current_stream(self.device)
+        side = self._copy_stream()
+        for b in range(B):
+            for c0, c1 in self._coil_groups():
+                if self.uses_sense:
+                    img, sm = x[b:b + 1], self._smaps[c0:c1]
+                else:
+                    img, sm = x[b * C + c0:b * C + c1], None
+                self._plan.op(img, sm, dev_k[b, c0:c1], 1, c1 - c0, self.inv_norm_factor,
+                              isign=self._isign)
+                side.wait_stream(main)
+                with torch.cuda.stream(side):
+                    out[b, c0:c1].copy_(dev_k[b, c0:c1], non_blocking=True)
+        side.synchronize()
+        return out.numpy()
 
     def _op(self, image, coeffs):
         """Unnormalised type-2 transforms of an (n, *shape) image stack."""

@@ -206,6 +206,34 @@ def test_array_types_and_no_mutation(gpu_pkg, golden):
     assert x_gpu.is_cuda and x_gpu.shape == shape
 
 
+def test_numpy_results_pinned_and_chained(gpu_pkg, golden, monkeypatch):
+    """numpy results come back in page-locked memory, stay valid across later
+    calls, and feed the next call (asynchronous copy) with the values of the
+    device path; the pageable route gives the same values."""
+    from mrinufft_gb300 import _array
+
+    s, shape = _case(golden, "random2D")
+    op = gpu_pkg.MRIGB300(s, shape)
+    img = golden["random2D__img"]
+    y = op.op(img)
+    assert isinstance(y, np.ndarray) and torch.from_numpy(y).is_pinned()
+    x = op.adj_op(y)
+    assert isinstance(x, np.ndarray) and torch.from_numpy(x).is_pinned()
+    t = torch.from_numpy(img).cuda()
+    x_dev = op.adj_op(op.op(t)).cpu().numpy()
+    # the adjoint's float atomics may add in another order from run to run
+    np.testing.assert_allclose(x, x_dev, rtol=1e-5, atol=1e-6)
+    y_copy = y.copy()
+    for _ in range(3):
+        op.adj_op(op.op(img * 2))
+    np.testing.assert_array_equal(y, y_copy)
+    monkeypatch.setattr(_array, "PINNED_RESULTS", False)
+    y2 = op.op(img)
+    assert not torch.from_numpy(y2).is_pinned()
+    np.testing.assert_array_equal(y2, y_copy)
+    np.testing.assert_allclose(op.adj_op(y2), x, rtol=1e-5, atol=1e-6)
+
+
 def test_no_samples(gpu_pkg):
     op = gpu_pkg.MRIGB300(np.zeros((0, 2), np.float32), (16, 16))
     y = op.op(np.ones((16, 16), np.complex64))
