@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "gbn_batch.cuh"
+#include "gbn_fft256.cuh"
 #include "gbn_internal.cuh"
 #include "gbn_passes.cuh"
 #include "gbn_sort.cuh"
@@ -194,6 +195,11 @@ struct gbn_plan_s {
   bool prune = false;
   cufftHandle pl_lo = 0, pl_span = 0, pl_hi = 0, pl_x = 0;
 
+  // 256^3 fine grids: the fused pruned line transforms of gbn_fft256.cu
+  // replace the pad pass, cuFFT and the crop pass of op / adj / dc
+  bool fft256 = false;
+  float2* tw256 = nullptr;  // W256^k table
+
   // per-stage CUDA-event timing (gbn_profile) and kernel launch count
   bool prof = false;
   std::vector<cudaEvent_t> evpool;
@@ -219,6 +225,7 @@ struct gbn_plan_s {
     for (int d = 0; d < 3; ++d) dev_free(dec[d]);
     dev_free(fine);
     dev_free(kbuf);
+    dev_free(tw256);
     free_points();
     free_bins();
     dev_free(sb.d_total);
@@ -432,6 +439,28 @@ void run_crop(gbn_plan p, const CropArgs& a, cudaStream_t st) {
   Span span(p, GBN_STAGE_CROP, st);
   ck(launch_crop(a, st), "crop pass");
   p->launches++;
+}
+// op: pad + forward transform (fused line transforms on 256^3 grids)
+void run_pad_fft(gbn_plan p, const PadArgs& a, int isign, cudaStream_t st) {
+  if (p->fft256) {
+    Span span(p, GBN_STAGE_FFT, st);
+    ck(launch_fft256_op(a, p->tw256, isign, st), "fused pad + transform");
+    p->launches += 3;
+    return;
+  }
+  run_pad(p, a, st);
+  p->exec_fft(a.ntr, p->fine, isign, st, 1);
+}
+// adjoint: inverse transform + crop
+void run_fft_crop(gbn_plan p, const CropArgs& a, int isign, cudaStream_t st) {
+  if (p->fft256) {
+    Span span(p, GBN_STAGE_FFT, st);
+    ck(launch_fft256_adj(a, p->fine, p->tw256, isign, st), "fused transform + crop");
+    p->launches += 3;
+    return;
+  }
+  p->exec_fft(a.ntr, p->fine, isign, st, 2);
+  run_crop(p, a, st);
 }
 void run_zero(gbn_plan p, float2* dst, size_t cells, cudaStream_t st) {
   Span span(p, GBN_STAGE_ZERO, st);
@@ -656,6 +685,14 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
     {
       const char* e = std::getenv("GBN_FFT_PRUNE");
       p->prune = dim == 3 && !spread_only && g.nf[0] > g.n[0] && !(e && std::atoi(e) == 0);
+      const char* f = std::getenv("GBN_FUSED_FFT");
+      p->fft256 = !spread_only && fft256_fits(g) && !(f && std::atoi(f) == 0);
+      if (p->fft256) {
+        std::vector<float> t = fft256_twiddles();
+        p->tw256 = dev_alloc<float2>(256, p->bytes, "transform twiddles");
+        ck(cudaMemcpy(p->tw256, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice),
+           "copy transform twiddles");
+      }
     }
     p->fine = dev_alloc<float2>((size_t)ntrans * g.G, p->bytes, "fine grid");
     p->setup_bins();
@@ -821,8 +858,7 @@ int gbn_op(gbn_plan p, const void* img, const void* smaps, void* ksp, int B, int
     for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
       PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                      : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
-      run_pad(p, pa, st);
-      p->exec_fft(T, p->fine, isign, st, 1);
+      run_pad_fft(p, pa, isign, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       run_interp(p, interp_args(p, p->fine, y + row * p->M, T, scale, INTERP_STORE), st);
     });
@@ -854,11 +890,10 @@ int gbn_adj(gbn_plan p, const void* ksp, const float* density, const void* smaps
       run_zero(p, p->fine, (size_t)T * g.G, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       run_spread(p, spread_args(p, y + row * p->M, density, p->fine, T, 1.0f), st);
-      p->exec_fft(T, p->fine, isign, st, 2);
       CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, x + (int64_t)b * g.Nimg, T,
                                   c0 > 0, scale)
                       : crop_args(p, nullptr, x + (int64_t)c0 * g.Nimg, T, 0, scale);
-      run_crop(p, ca, st);
+      run_fft_crop(p, ca, isign, st);
     });
   });
 }
@@ -888,8 +923,7 @@ int gbn_dc(gbn_plan p, const void* img, const void* obs, const float* density,
     for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
       PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                      : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
-      run_pad(p, pa, st);
-      p->exec_fft(T, p->fine, -1, st, 1);
+      run_pad_fft(p, pa, -1, st);
       int64_t row = s ? (int64_t)b * C + c0 : c0;
       InterpArgs ia = interp_args(p, p->fine, p->kbuf, T, scale, INTERP_RESID);
       ia.obs = yo + row * p->M;
@@ -897,11 +931,10 @@ int gbn_dc(gbn_plan p, const void* img, const void* obs, const float* density,
       run_interp(p, ia, st);
       run_zero(p, p->fine, (size_t)T * g.G, st);
       run_spread(p, spread_args(p, p->kbuf, nullptr, p->fine, T, 1.0f), st);
-      p->exec_fft(T, p->fine, +1, st, 2);
       CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, gr + (int64_t)b * g.Nimg, T,
                                   c0 > 0, scale)
                       : crop_args(p, nullptr, gr + (int64_t)c0 * g.Nimg, T, 0, scale);
-      run_crop(p, ca, st);
+      run_fft_crop(p, ca, +1, st);
     });
   });
 }
@@ -932,8 +965,7 @@ static void grad_traj_common(gbn_plan p, const float2* img, const float2* s, con
   for_each_pass(p, s != nullptr, B, C, [&](int b, int c0, int T) {
     PadArgs pa = s ? pad_args(p, img + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, adjoint)
                    : pad_args(p, img + (int64_t)c0 * g.Nimg, nullptr, T, adjoint);
-    run_pad(p, pa, st);
-    p->exec_fft(T, p->fine, adjoint ? +1 : -1, st, 1);
+    run_pad_fft(p, pa, adjoint ? +1 : -1, st);
     int64_t row = s ? (int64_t)b * C + c0 : c0;
     GradArgs ga{};
     ga.g = g;
@@ -1168,19 +1200,17 @@ void toep_apply(gbn_toep t, const void* img, const void* smaps, void* out, int B
     PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                    : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
     pa.dec[0] = pa.dec[1] = pa.dec[2] = nullptr;
-    run_pad(p, pa, st);
-    p->exec_fft(T, p->fine, -1, st, 1);
+    run_pad_fft(p, pa, -1, st);
     {
       Span span(p, GBN_STAGE_KMUL, st);
       ck(launch_kmul(p->fine, t->K, g.G, T, st), "Toeplitz multiply");
       p->launches++;
     }
-    p->exec_fft(T, p->fine, +1, st, 2);
     CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, o + (int64_t)b * g.Nimg, T,
                                 accumulate || c0 > 0, sc)
                     : crop_args(p, nullptr, o + (int64_t)c0 * g.Nimg, T, accumulate, sc);
     ca.dec[0] = ca.dec[1] = ca.dec[2] = nullptr;
-    run_crop(p, ca, st);
+    run_fft_crop(p, ca, +1, st);
   });
 }
 }  // namespace

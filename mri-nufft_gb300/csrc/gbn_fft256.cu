@@ -1,0 +1,399 @@
+// Pruned 3D transforms on 256^3 fine grids, fused with the pad and crop
+// passes.
+//
+// The image modes of an N-point axis occupy the fine indices [0, N - N/2)
+// and [256 - N/2, 256).  A type-2 transform (op) therefore starts from a
+// grid that is non-zero only on the (x mode, y mode, z mode) cells, and a
+// type-1 transform (adjoint) keeps only those cells of its result.  The
+// library's cuFFT path writes every fine cell in the pad pass and runs full
+// 2D transforms over the mode planes, then 1D transforms along x.  Here each
+// axis is a separate pass of 256-point line transforms that reads only the
+// lines and entries that can be non-zero and writes only the entries that a
+// later pass reads:
+//
+//   op      z lines of the (x mode, y mode) columns, pad fused into the
+//           loads (x * s * scale / phihat), 128 of 256 inputs per line;
+//           y lines of the x-mode planes (mode entries in, all out);
+//           x lines of every (y, z) (mode entries in, all out).
+//   adjoint x lines of every (y, z) (all in, mode entries out);
+//           y lines of the x-mode planes (all in, mode entries out);
+//           z lines of the (x mode, y mode) columns (all in, mode entries
+//           out), crop fused into the stores (divide by phihat, scale, and
+//           the SENSE coil combine sum_c conj(s_c) v_c over the pass's coils).
+//
+// For a 128^3 image this moves about 350 MB per coil and transform against
+// about 670 MB for the pad pass plus the pruned cuFFT passes.
+//
+// A 256-point line transform is two 16-point DFTs in registers with one
+// exchange through shared memory (four-step: n = 16 a + b, k = k1 + 16 k2):
+//   Y_b[k1] = sum_a x[16 a + b] W16^(a k1),   Z_b[k1] = Y_b[k1] W256^(b k1),
+//   X[k1 + 16 k2] = sum_b Z_b[k1] W16^(b k2).
+// A thread owns one (line, b) in the first step and one (line, k1) in the
+// second.  The 16-point DFT is radix 4 x 4.  The exponent sign is -1; a +1
+// transform conjugates its inputs and outputs.  The twiddles W256^(b k1)
+// come from a table computed in double precision on the host, laid out
+// [k1][b] so that lanes running over b read consecutive entries.
+//
+// Thread layouts (256 threads, 16 lines per CTA):
+//   z lines (contiguous in memory): lanes run over b (first step) or k1
+//     (second step) of two lines, so each global access is a 128-byte row
+//     segment; the exchange buffer [line][k1][b] has a row pitch of 17
+//     cells, which keeps both steps free of bank conflicts;
+//   x / y lines (stride 256 or 65536 cells): lanes run over 16 consecutive
+//     z columns, so each global access is again a 128-byte segment; the
+//     exchange buffer is [k1][b][z].
+#include "gbn_fft256.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace gbn {
+
+namespace {
+
+constexpr int kF256Lines = 16;       // lines per CTA
+constexpr int kF256Threads = 256;
+
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 f2conj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 f2scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// 4-point DFT, exponent sign -1, in place
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 t0 = f2add(a0, a2), t1 = f2sub(a0, a2), t2 = f2add(a1, a3), t3 = f2sub(a1, a3);
+  a0 = f2add(t0, t2);
+  a2 = f2sub(t0, t2);
+  a1 = make_float2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+  a3 = make_float2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+}
+
+// 16-point DFT, exponent sign -1: x[n] in natural order in, X[k] at x[pos16(k)] out
+__device__ __forceinline__ int pos16(int k) { return 4 * (k & 3) + (k >> 2); }
+
+__device__ __forceinline__ void dft16(float2 (&x)[16]) {
+  // W16^k = (cos(2 pi k / 16), -sin(2 pi k / 16))
+  constexpr float c1 = 0.92387953251128674f;  // cos(pi / 8)
+  constexpr float s1 = 0.38268343236508977f;  // sin(pi / 8)
+  constexpr float r2 = 0.70710678118654752f;  // sqrt(1 / 2)
+#pragma unroll
+  for (int r = 0; r < 4; ++r) dft4(x[r], x[r + 4], x[r + 8], x[r + 12]);
+  // x[r + 4 s] *= W16^(r s)
+  x[5] = f2mul(x[5], make_float2(c1, -s1));    // r 1, s 1
+  x[9] = f2mul(x[9], make_float2(r2, -r2));    // r 1, s 2
+  x[13] = f2mul(x[13], make_float2(s1, -c1));  // r 1, s 3
+  x[6] = f2mul(x[6], make_float2(r2, -r2));    // r 2, s 1
+  x[10] = make_float2(x[10].y, -x[10].x);      // r 2, s 2: W16^4 = -i
+  x[14] = f2mul(x[14], make_float2(-r2, -r2)); // r 2, s 3: W16^6
+  x[7] = f2mul(x[7], make_float2(s1, -c1));    // r 3, s 1: W16^3
+  x[11] = f2mul(x[11], make_float2(-r2, -r2)); // r 3, s 2: W16^6
+  x[15] = f2mul(x[15], make_float2(-c1, s1));  // r 3, s 3: W16^9
+#pragma unroll
+  for (int s = 0; s < 4; ++s) dft4(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+}
+
+// modes of an n-point axis on the 256-point fine axis
+__device__ __forceinline__ bool is_mode(int m, int n) {
+  const int h = n >> 1;
+  return m < n - h || m >= 256 - h;
+}
+__device__ __forceinline__ int mode_to_img(int m, int n) {  // image array index of fine index m
+  const int h = n >> 1;
+  return m < n - h ? m + h : m - 256 + h;
+}
+__device__ __forceinline__ int img_to_fine(int i, int n) {
+  const int k = i - (n >> 1);
+  return k < 0 ? k + 256 : k;
+}
+
+// ---------------------------------------------------------------- z lines, pad fused
+// blockIdx.x: 16 consecutive (ix, iy) image columns; blockIdx.y: transform
+__global__ void __launch_bounds__(kF256Threads)
+f256_pad_z_kernel(PadArgs a, const float2* __restrict__ tw, int conj) {
+  __shared__ float2 s_tw[256];
+  __shared__ float2 s_x[kF256Lines * 16 * 17];
+  const Geom& g = a.g;
+  const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+  s_tw[threadIdx.x] = tw[threadIdx.x];
+  const int b = threadIdx.x & 15, l = threadIdx.x >> 4;
+  const int line = blockIdx.x * kF256Lines + l;
+  const bool valid = line < n0 * n1;
+  const int ix = valid ? line / n1 : 0, iy = valid ? line - ix * n1 : 0;
+  const int c = blockIdx.y;
+  const int64_t irow = ((int64_t)ix * n1 + iy) * n2;
+  const float2* img = a.smaps ? a.img : a.img + (int64_t)c * g.Nimg;
+  const float2* sm = a.smaps ? a.smaps + (int64_t)c * g.Nimg : nullptr;
+  float f0 = a.scale;
+  if (a.dec[0]) f0 *= a.dec[0][ix];
+  if (a.dec[1]) f0 *= a.dec[1][iy];
+  float2 x[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int m = 16 * q + b;
+    float2 v = make_float2(0.f, 0.f);
+    if (valid && is_mode(m, n2)) {
+      const int i2 = mode_to_img(m, n2);
+      v = img[irow + i2];
+      if (a.conj_in) v = f2conj(v);
+      if (sm) {
+        float2 s = sm[irow + i2];
+        if (a.conj_in) s = f2conj(s);
+        v = f2mul(v, s);
+      }
+      v = f2scale(v, a.dec[2] ? f0 * a.dec[2][i2] : f0);
+      if (conj) v = f2conj(v);
+    }
+    x[q] = v;
+  }
+  __syncthreads();  // twiddle table
+  dft16(x);
+  float2* row = s_x + l * (16 * 17);
+#pragma unroll
+  for (int k1 = 0; k1 < 16; ++k1) row[k1 * 17 + b] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
+  __syncthreads();
+  const int k1 = b;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) x[q] = row[k1 * 17 + q];
+  dft16(x);
+  if (!valid) return;
+  float2* out = a.fine + (int64_t)c * g.G +
+                ((int64_t)img_to_fine(ix, n0) * 256 + img_to_fine(iy, n1)) * 256 + k1;
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) {
+    const float2 v = x[pos16(k2)];
+    out[16 * k2] = conj ? f2conj(v) : v;
+  }
+}
+
+// ---------------------------------------------------------------- x / y lines
+struct F256Lines {
+  float2* data;       // ntr grids of G cells
+  int64_t G;
+  int64_t line_stride;   // cells between consecutive entries of a line
+  int64_t outer_stride;  // cells between consecutive outer indices
+  int outer_modes;       // outer index o is an image index of an n_outer-point axis
+  int n_outer;
+  int n_axis;            // image size along the transformed axis
+  int in_prune;          // only mode entries are read (the others are zero)
+  int out_prune;         // only mode entries are written
+  int conj;
+  const float2* tw;
+};
+
+// blockIdx.x: 16 consecutive z columns; blockIdx.y: outer index; blockIdx.z: transform
+template <int MINB>
+__global__ void __launch_bounds__(kF256Threads, MINB) f256_lines_kernel(F256Lines a) {
+  __shared__ float2 s_tw[256];
+  __shared__ float2 s_x[16 * 16 * kF256Lines];
+  s_tw[threadIdx.x] = a.tw[threadIdx.x];
+  const int l = threadIdx.x & 15, b = threadIdx.x >> 4;
+  const int z = blockIdx.x * kF256Lines + l;
+  const int o = a.outer_modes ? img_to_fine(blockIdx.y, a.n_outer) : (int)blockIdx.y;
+  float2* base = a.data + (int64_t)blockIdx.z * a.G + o * a.outer_stride + z;
+  float2 x[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int m = 16 * q + b;
+    float2 v = make_float2(0.f, 0.f);
+    if (!a.in_prune || is_mode(m, a.n_axis)) {
+      v = base[m * a.line_stride];
+      if (a.conj) v = f2conj(v);
+    }
+    x[q] = v;
+  }
+  __syncthreads();  // twiddle table
+  dft16(x);
+#pragma unroll
+  for (int k1 = 0; k1 < 16; ++k1) s_x[(k1 * 16 + b) * 16 + l] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
+  __syncthreads();
+  const int k1 = b;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) x[q] = s_x[(k1 * 16 + q) * 16 + l];
+  dft16(x);
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) {
+    const int k = k1 + 16 * k2;
+    if (!a.out_prune || is_mode(k, a.n_axis)) {
+      const float2 v = x[pos16(k2)];
+      base[k * a.line_stride] = a.conj ? f2conj(v) : v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- z lines, crop fused
+// blockIdx.x: 16 consecutive (ix, iy) image columns; the CTA runs every
+// transform of the pass and, with coil maps, sums them into one image
+constexpr size_t kCropSmem = (256 + kF256Lines * 16 * 17 + kF256Lines * 16 * 16) * sizeof(float2);
+
+template <int MINB>
+__global__ void __launch_bounds__(kF256Threads, MINB)
+f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
+  // dynamic: twiddles, the exchange buffer, and the coil sums [line][k2][k1]
+  // (thread (line, k1) owns its 16 entries)
+  extern __shared__ float2 s_dyn[];
+  float2* const s_tw = s_dyn;
+  float2* const s_x = s_tw + 256;
+  float2* const s_acc = s_x + kF256Lines * 16 * 17;
+  const Geom& g = a.g;
+  const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+  s_tw[threadIdx.x] = tw[threadIdx.x];
+  const int b = threadIdx.x & 15, l = threadIdx.x >> 4;
+  const int line = blockIdx.x * kF256Lines + l;
+  const bool valid = line < n0 * n1;
+  const int ix = valid ? line / n1 : 0, iy = valid ? line - ix * n1 : 0;
+  const int64_t irow = ((int64_t)ix * n1 + iy) * n2;
+  const int64_t frow = ((int64_t)img_to_fine(ix, n0) * 256 + img_to_fine(iy, n1)) * 256;
+  float f0 = a.scale;
+  if (a.dec[0]) f0 *= a.dec[0][ix];
+  if (a.dec[1]) f0 *= a.dec[1][iy];
+  float2* row = s_x + l * (16 * 17);
+  const int k1 = b;
+  float2* acc = s_acc + l * 256 + k1;  // entry k2 at acc[16 * k2]
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) acc[16 * k2] = make_float2(0.f, 0.f);
+  for (int c = 0; c < a.ntr; ++c) {
+    const float2* in = a.fine + (int64_t)c * g.G + frow;
+    float2 x[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float2 v = valid ? in[16 * q + b] : make_float2(0.f, 0.f);
+      x[q] = conj ? f2conj(v) : v;
+    }
+    __syncthreads();  // twiddle table; the previous transform's exchange reads are done
+    dft16(x);
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) row[kk * 17 + b] = f2mul(x[pos16(kk)], s_tw[kk * 16 + b]);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) x[q] = row[k1 * 17 + q];
+    dft16(x);
+    if (!valid) continue;
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+      const int k = k1 + 16 * k2;
+      if (!is_mode(k, n2)) continue;
+      const int i2 = mode_to_img(k, n2);
+      float2 v = x[pos16(k2)];
+      if (conj) v = f2conj(v);
+      if (a.smaps) {
+        const float2 s = a.smaps[(int64_t)c * g.Nimg + irow + i2];
+        const float2 o = acc[16 * k2];
+        acc[16 * k2] = make_float2(o.x + s.x * v.x + s.y * v.y, o.y + s.x * v.y - s.y * v.x);
+      } else {
+        const float f = a.dec[2] ? f0 * a.dec[2][i2] : f0;
+        float2 r = f2scale(v, f);
+        float2* dst = a.out + (int64_t)c * g.Nimg + irow + i2;
+        if (a.accumulate) r = f2add(r, *dst);
+        *dst = r;
+      }
+    }
+  }
+  if (!a.smaps || !valid) return;
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) {
+    const int k = k1 + 16 * k2;
+    if (!is_mode(k, n2)) continue;
+    const int i2 = mode_to_img(k, n2);
+    const float f = a.dec[2] ? f0 * a.dec[2][i2] : f0;
+    float2 r = f2scale(acc[16 * k2], f);
+    float2* dst = a.out + irow + i2;
+    if (a.accumulate) r = f2add(r, *dst);
+    *dst = r;
+  }
+}
+
+}  // namespace
+
+bool fft256_fits(const Geom& g) {
+  return g.dim == 3 && g.nf[0] == 256 && g.nf[1] == 256 && g.nf[2] == 256;
+}
+
+std::vector<float> fft256_twiddles() {
+  // entry k1 * 16 + b: W256^(b k1) = exp(-2 pi i b k1 / 256), as (re, im)
+  std::vector<float> t(512);
+  const double pi = 3.14159265358979323846;
+  for (int k1 = 0; k1 < 16; ++k1)
+    for (int b = 0; b < 16; ++b) {
+      const int e = k1 * 16 + b;
+      t[2 * e] = (float)std::cos(2.0 * pi * b * k1 / 256.0);
+      t[2 * e + 1] = (float)-std::sin(2.0 * pi * b * k1 / 256.0);
+    }
+  return t;
+}
+
+namespace {
+// 4 CTAs per SM (64 registers, a few bytes of spills) measured 5 % faster
+// than 3 CTAs at 80 registers on the 128^3 passes
+void lines(const F256Lines& a, dim3 grid, cudaStream_t st) {
+  f256_lines_kernel<4><<<grid, kF256Threads, 0, st>>>(a);
+}
+}  // namespace
+
+cudaError_t launch_fft256_op(const PadArgs& pa, const float2* tw, int isign, cudaStream_t st) {
+  const Geom& g = pa.g;
+  const int conj = isign > 0;
+  const int nl = g.n[0] * g.n[1];
+  f256_pad_z_kernel<<<dim3((nl + kF256Lines - 1) / kF256Lines, pa.ntr), kF256Threads, 0, st>>>(
+      pa, tw, conj);
+  F256Lines y{};
+  y.data = pa.fine;
+  y.G = g.G;
+  y.line_stride = 256;
+  y.outer_stride = 256 * 256;
+  y.outer_modes = 1;
+  y.n_outer = g.n[0];
+  y.n_axis = g.n[1];
+  y.in_prune = 1;
+  y.out_prune = 0;
+  y.conj = conj;
+  y.tw = tw;
+  lines(y, dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
+  F256Lines x = y;
+  x.line_stride = 256 * 256;
+  x.outer_stride = 256;
+  x.outer_modes = 0;
+  x.n_outer = 256;
+  x.n_axis = g.n[0];
+  lines(x, dim3(256 / kF256Lines, 256, pa.ntr), st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fft256_adj(const CropArgs& ca, float2* fine, const float2* tw, int isign,
+                              cudaStream_t st) {
+  const Geom& g = ca.g;
+  const int conj = isign > 0;
+  F256Lines x{};
+  x.data = fine;
+  x.G = g.G;
+  x.line_stride = 256 * 256;
+  x.outer_stride = 256;
+  x.outer_modes = 0;
+  x.n_outer = 256;
+  x.n_axis = g.n[0];
+  x.in_prune = 0;
+  x.out_prune = 1;
+  x.conj = conj;
+  x.tw = tw;
+  lines(x, dim3(256 / kF256Lines, 256, ca.ntr), st);
+  F256Lines y = x;
+  y.line_stride = 256;
+  y.outer_stride = 256 * 256;
+  y.outer_modes = 1;
+  y.n_outer = g.n[0];
+  y.n_axis = g.n[1];
+  lines(y, dim3(256 / kF256Lines, g.n[0], ca.ntr), st);
+  const int nl = g.n[0] * g.n[1];
+  const unsigned nb = (nl + kF256Lines - 1) / kF256Lines;
+  // coil sums in shared memory: 3 CTAs per SM (69 against 86 us with the
+  // sums in registers at 2 CTAs per SM, 4 coils of a 128^3 image)
+  auto k = f256_z_crop_kernel<3>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
+  if (e != cudaSuccess) return e;
+  k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, conj);
+  return cudaGetLastError();
+}
+
+}  // namespace gbn

@@ -10,7 +10,9 @@ warp-cooperative, tiles), coils per pass (``GBN_INTERP_CG``,
 ``GBN_SPREAD_CG``), the interp CTA size (``GBN_INTERP_THREADS``), the bin
 sizes (``GBN_BINS2`` / ``GBN_BINS3``) and the pruned 3D FFT
 (``GBN_FFT_PRUNE``).  Each setting runs SENSE op, adj and data consistency
-in 2D and 3D (and a calibrationless case) with relative l2 <= 1e-4.
+in 2D and 3D (and a calibrationless case) with relative l2 <= 1e-4.  The
+fused 256^3 transforms (``GBN_FUSED_FFT``) need 256-point fine axes and are
+covered by test_gpu_fft256.py.
 """
 
 import os
