@@ -1200,16 +1200,22 @@ void toep_apply(gbn_toep t, const void* img, const void* smaps, void* out, int B
     PadArgs pa = s ? pad_args(p, x + (int64_t)b * g.Nimg, s + (int64_t)c0 * g.Nimg, T, 0)
                    : pad_args(p, x + (int64_t)c0 * g.Nimg, nullptr, T, 0);
     pa.dec[0] = pa.dec[1] = pa.dec[2] = nullptr;
+    CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, o + (int64_t)b * g.Nimg, T,
+                                accumulate || c0 > 0, sc)
+                    : crop_args(p, nullptr, o + (int64_t)c0 * g.Nimg, T, accumulate, sc);
+    ca.dec[0] = ca.dec[1] = ca.dec[2] = nullptr;
+    if (p->fft256) {  // the x transforms and the multiply in one pass over the lines
+      Span span(p, GBN_STAGE_FFT, st);
+      ck(launch_fft256_gram(pa, ca, t->K, p->tw256, st), "fused Toeplitz Gram");
+      p->launches += 5;
+      return;
+    }
     run_pad_fft(p, pa, -1, st);
     {
       Span span(p, GBN_STAGE_KMUL, st);
       ck(launch_kmul(p->fine, t->K, g.G, T, st), "Toeplitz multiply");
       p->launches++;
     }
-    CropArgs ca = s ? crop_args(p, s + (int64_t)c0 * g.Nimg, o + (int64_t)b * g.Nimg, T,
-                                accumulate || c0 > 0, sc)
-                    : crop_args(p, nullptr, o + (int64_t)c0 * g.Nimg, T, accumulate, sc);
-    ca.dec[0] = ca.dec[1] = ca.dec[2] = nullptr;
     run_fft_crop(p, ca, +1, st);
   });
 }

@@ -305,6 +305,63 @@ f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
   }
 }
 
+// ---------------------------------------------------------------- x lines of the Toeplitz Gram
+// Forward x transform (x-mode entries in), multiply by the real kernel K,
+// inverse x transform (x-mode entries out) of every (y, z) line, for every
+// transform of the pass, without writing the full grid.  After the forward
+// transform's second step thread (z, k1) holds X[k1 + 16 k2], k2 = 0 .. 15,
+// which are exactly the inputs x[16 a + b] (a = k2) of the inverse
+// transform's first step for b = k1, so the two transforms share one layout.
+// blockIdx.x: 16 consecutive z columns; blockIdx.y: y
+__global__ void __launch_bounds__(kF256Threads, 3)
+f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __restrict__ K,
+                   const float2* __restrict__ tw) {
+  __shared__ float2 s_tw[256];
+  __shared__ float2 s_x[16 * 16 * kF256Lines];
+  s_tw[threadIdx.x] = tw[threadIdx.x];
+  const int l = threadIdx.x & 15, b = threadIdx.x >> 4;
+  const int z = blockIdx.x * kF256Lines + l;
+  const int64_t col = (int64_t)blockIdx.y * 256 + z;
+  constexpr int64_t XS = 256 * 256;  // x stride
+  float kk[16];  // K at x = b + 16 k2 (b is k1 in the forward transform's second step)
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) kk[k2] = K[(b + 16 * k2) * XS + col];
+  for (int c = 0; c < ntr; ++c) {
+    float2* base = data + (int64_t)c * G + col;
+    float2 x[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int m = 16 * q + b;
+      x[q] = is_mode(m, n0) ? base[m * XS] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();  // twiddles; the previous transform's exchange reads are done
+    dft16(x);
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) s_x[(k1 * 16 + b) * 16 + l] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
+    __syncthreads();
+    // thread (z, k1 = b): X[k1 + 16 k2] -> conj(K X) as the inverse transform's x[16 k2 + k1]
+    float2 y[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) y[q] = s_x[(b * 16 + q) * 16 + l];
+    dft16(y);
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) x[k2] = f2conj(f2scale(y[pos16(k2)], kk[k2]));
+    dft16(x);
+    __syncthreads();  // every thread has read its forward exchange entries
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) s_x[(k1 * 16 + b) * 16 + l] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) y[q] = s_x[(b * 16 + q) * 16 + l];
+    dft16(y);
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+      const int k = b + 16 * k2;
+      if (is_mode(k, n0)) base[k * XS] = f2conj(y[pos16(k2)]);
+    }
+  }
+}
+
 }  // namespace
 
 bool fft256_fits(const Geom& g) {
@@ -393,6 +450,39 @@ cudaError_t launch_fft256_adj(const CropArgs& ca, float2* fine, const float2* tw
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
   if (e != cudaSuccess) return e;
   k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, conj);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fft256_gram(const PadArgs& pa, const CropArgs& ca, const float* K,
+                               const float2* tw, cudaStream_t st) {
+  const Geom& g = pa.g;
+  const int nl = g.n[0] * g.n[1];
+  f256_pad_z_kernel<<<dim3((nl + kF256Lines - 1) / kF256Lines, pa.ntr), kF256Threads, 0, st>>>(
+      pa, tw, 0);
+  F256Lines y{};
+  y.data = pa.fine;
+  y.G = g.G;
+  y.line_stride = 256;
+  y.outer_stride = 256 * 256;
+  y.outer_modes = 1;
+  y.n_outer = g.n[0];
+  y.n_axis = g.n[1];
+  y.in_prune = 1;
+  y.out_prune = 0;
+  y.conj = 0;
+  y.tw = tw;
+  lines(y, dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
+  f256_x_kmul_kernel<<<dim3(256 / kF256Lines, 256), kF256Threads, 0, st>>>(pa.fine, g.G, pa.ntr,
+                                                                            g.n[0], K, tw);
+  y.in_prune = 0;
+  y.out_prune = 1;
+  y.conj = 1;
+  lines(y, dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
+  const unsigned nb = (nl + kF256Lines - 1) / kF256Lines;
+  auto k = f256_z_crop_kernel<3>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
+  if (e != cudaSuccess) return e;
+  k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, 1);
   return cudaGetLastError();
 }
 

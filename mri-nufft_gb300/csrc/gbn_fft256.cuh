@@ -23,4 +23,11 @@ cudaError_t launch_fft256_op(const PadArgs& pa, const float2* tw, int isign, cud
 cudaError_t launch_fft256_adj(const CropArgs& ca, float2* fine, const float2* tw, int isign,
                               cudaStream_t st);
 
+// Toeplitz Gram of a pass (pa.ntr = ca.ntr transforms): pad, forward
+// transform, multiply by the real circulant spectrum K (256^3), inverse
+// transform and crop, with the x transforms and the multiply in one pass
+// over the (y, z) lines; the fine grids hold only intermediate line data.
+cudaError_t launch_fft256_gram(const PadArgs& pa, const CropArgs& ca, const float* K,
+                               const float2* tw, cudaStream_t st);
+
 }  // namespace gbn
