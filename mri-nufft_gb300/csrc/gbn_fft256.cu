@@ -109,8 +109,26 @@ __device__ __forceinline__ int img_to_fine(int i, int n) {
   return k < 0 ? k + 256 : k;
 }
 
+// Entry m = 16 q + b of a line, for the mode sets of the transformed axis:
+// kAll (every entry), kHalf (n = 128: the modes are the rows q < 4 and
+// q >= 12, known at compile time in the unrolled loops), kModes (any n <= 256).
+enum : int { kAll = 0, kHalf = 1, kModes = 2 };
+template <int SET>
+__device__ __forceinline__ bool entry_on(int q, int b, int n) {
+  if (SET == kAll) return true;
+  if (SET == kHalf) return q < 4 || q >= 12;
+  return is_mode(16 * q + b, n);
+}
+template <int SET>
+__device__ __forceinline__ int entry_img(int q, int b, int n) {  // image index of a mode entry
+  if (SET == kHalf) return q < 4 ? 16 * q + b + 64 : 16 * q + b - 192;
+  return mode_to_img(16 * q + b, n);
+}
+
 // ---------------------------------------------------------------- z lines, pad fused
-// blockIdx.x: 16 consecutive (ix, iy) image columns; blockIdx.y: transform
+// blockIdx.x: 16 consecutive (ix, iy) image columns; blockIdx.y: transform;
+// SET: the z modes (kHalf for n2 = 128, else kModes)
+template <int SET>
 __global__ void __launch_bounds__(kF256Threads)
 f256_pad_z_kernel(PadArgs a, const float2* __restrict__ tw, int conj) {
   __shared__ float2 s_tw[256];
@@ -132,10 +150,9 @@ f256_pad_z_kernel(PadArgs a, const float2* __restrict__ tw, int conj) {
   float2 x[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
-    const int m = 16 * q + b;
     float2 v = make_float2(0.f, 0.f);
-    if (valid && is_mode(m, n2)) {
-      const int i2 = mode_to_img(m, n2);
+    if (valid && entry_on<SET>(q, b, n2)) {
+      const int i2 = entry_img<SET>(q, b, n2);
       v = img[irow + i2];
       if (a.conj_in) v = f2conj(v);
       if (sm) {
@@ -184,7 +201,8 @@ struct F256Lines {
 };
 
 // blockIdx.x: 16 consecutive z columns; blockIdx.y: outer index; blockIdx.z: transform
-template <int MINB>
+// IN / OUT: the entries read / written (kAll, kHalf, kModes of n_axis)
+template <int MINB, int IN, int OUT>
 __global__ void __launch_bounds__(kF256Threads, MINB) f256_lines_kernel(F256Lines a) {
   __shared__ float2 s_tw[256];
   __shared__ float2 s_x[16 * 16 * kF256Lines];
@@ -196,10 +214,9 @@ __global__ void __launch_bounds__(kF256Threads, MINB) f256_lines_kernel(F256Line
   float2 x[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
-    const int m = 16 * q + b;
     float2 v = make_float2(0.f, 0.f);
-    if (!a.in_prune || is_mode(m, a.n_axis)) {
-      v = base[m * a.line_stride];
+    if (entry_on<IN>(q, b, a.n_axis)) {
+      v = base[(16 * q + b) * a.line_stride];
       if (a.conj) v = f2conj(v);
     }
     x[q] = v;
@@ -215,10 +232,9 @@ __global__ void __launch_bounds__(kF256Threads, MINB) f256_lines_kernel(F256Line
   dft16(x);
 #pragma unroll
   for (int k2 = 0; k2 < 16; ++k2) {
-    const int k = k1 + 16 * k2;
-    if (!a.out_prune || is_mode(k, a.n_axis)) {
+    if (entry_on<OUT>(k2, k1, a.n_axis)) {
       const float2 v = x[pos16(k2)];
-      base[k * a.line_stride] = a.conj ? f2conj(v) : v;
+      base[(k1 + 16 * k2) * a.line_stride] = a.conj ? f2conj(v) : v;
     }
   }
 }
@@ -228,7 +244,7 @@ __global__ void __launch_bounds__(kF256Threads, MINB) f256_lines_kernel(F256Line
 // transform of the pass and, with coil maps, sums them into one image
 constexpr size_t kCropSmem = (256 + kF256Lines * 16 * 17 + kF256Lines * 16 * 16) * sizeof(float2);
 
-template <int MINB>
+template <int MINB, int SET>
 __global__ void __launch_bounds__(kF256Threads, MINB)
 f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
   // dynamic: twiddles, the exchange buffer, and the coil sums [line][k2][k1]
@@ -273,9 +289,8 @@ f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
     if (!valid) continue;
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
-      const int k = k1 + 16 * k2;
-      if (!is_mode(k, n2)) continue;
-      const int i2 = mode_to_img(k, n2);
+      if (!entry_on<SET>(k2, k1, n2)) continue;
+      const int i2 = entry_img<SET>(k2, k1, n2);
       float2 v = x[pos16(k2)];
       if (conj) v = f2conj(v);
       if (a.smaps) {
@@ -294,9 +309,8 @@ f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
   if (!a.smaps || !valid) return;
 #pragma unroll
   for (int k2 = 0; k2 < 16; ++k2) {
-    const int k = k1 + 16 * k2;
-    if (!is_mode(k, n2)) continue;
-    const int i2 = mode_to_img(k, n2);
+    if (!entry_on<SET>(k2, k1, n2)) continue;
+    const int i2 = entry_img<SET>(k2, k1, n2);
     const float f = a.dec[2] ? f0 * a.dec[2][i2] : f0;
     float2 r = f2scale(acc[16 * k2], f);
     float2* dst = a.out + irow + i2;
@@ -313,6 +327,7 @@ f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
 // which are exactly the inputs x[16 a + b] (a = k2) of the inverse
 // transform's first step for b = k1, so the two transforms share one layout.
 // blockIdx.x: 16 consecutive z columns; blockIdx.y: y
+template <int SET>
 __global__ void __launch_bounds__(kF256Threads, 3)
 f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __restrict__ K,
                    const float2* __restrict__ tw) {
@@ -330,10 +345,8 @@ f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __rest
     float2* base = data + (int64_t)c * G + col;
     float2 x[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int m = 16 * q + b;
-      x[q] = is_mode(m, n0) ? base[m * XS] : make_float2(0.f, 0.f);
-    }
+    for (int q = 0; q < 16; ++q)
+      x[q] = entry_on<SET>(q, b, n0) ? base[(16 * q + b) * XS] : make_float2(0.f, 0.f);
     __syncthreads();  // twiddles; the previous transform's exchange reads are done
     dft16(x);
 #pragma unroll
@@ -355,10 +368,8 @@ f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __rest
     for (int q = 0; q < 16; ++q) y[q] = s_x[(b * 16 + q) * 16 + l];
     dft16(y);
 #pragma unroll
-    for (int k2 = 0; k2 < 16; ++k2) {
-      const int k = b + 16 * k2;
-      if (is_mode(k, n0)) base[k * XS] = f2conj(y[pos16(k2)]);
-    }
+    for (int k2 = 0; k2 < 16; ++k2)
+      if (entry_on<SET>(k2, b, n0)) base[(b + 16 * k2) * XS] = f2conj(y[pos16(k2)]);
   }
 }
 
@@ -385,43 +396,55 @@ namespace {
 // 4 CTAs per SM (64 registers, a few bytes of spills) measured 5 % faster
 // than 3 CTAs at 80 registers on the 128^3 passes
 void lines(const F256Lines& a, dim3 grid, cudaStream_t st) {
-  f256_lines_kernel<4><<<grid, kF256Threads, 0, st>>>(a);
+  const bool half = a.n_axis == 128;
+  if (a.in_prune) {
+    if (half) f256_lines_kernel<4, kHalf, kAll><<<grid, kF256Threads, 0, st>>>(a);
+    else f256_lines_kernel<4, kModes, kAll><<<grid, kF256Threads, 0, st>>>(a);
+  } else if (a.out_prune) {
+    if (half) f256_lines_kernel<4, kAll, kHalf><<<grid, kF256Threads, 0, st>>>(a);
+    else f256_lines_kernel<4, kAll, kModes><<<grid, kF256Threads, 0, st>>>(a);
+  } else {
+    f256_lines_kernel<4, kAll, kAll><<<grid, kF256Threads, 0, st>>>(a);
+  }
 }
-}  // namespace
 
-cudaError_t launch_fft256_op(const PadArgs& pa, const float2* tw, int isign, cudaStream_t st) {
-  const Geom& g = pa.g;
-  const int conj = isign > 0;
-  const int nl = g.n[0] * g.n[1];
-  f256_pad_z_kernel<<<dim3((nl + kF256Lines - 1) / kF256Lines, pa.ntr), kF256Threads, 0, st>>>(
-      pa, tw, conj);
+void pad_z(const PadArgs& pa, const float2* tw, int conj, cudaStream_t st) {
+  const int nl = pa.g.n[0] * pa.g.n[1];
+  const dim3 grid((nl + kF256Lines - 1) / kF256Lines, pa.ntr);
+  if (pa.g.n[2] == 128) f256_pad_z_kernel<kHalf><<<grid, kF256Threads, 0, st>>>(pa, tw, conj);
+  else f256_pad_z_kernel<kModes><<<grid, kF256Threads, 0, st>>>(pa, tw, conj);
+}
+
+// coil sums in shared memory: 3 CTAs per SM (69 against 86 us with the sums
+// in registers at 2 CTAs per SM, 4 coils of a 128^3 image); the runtime mode
+// test (kModes) also for n2 = 128: the kHalf instance measured 90 us
+cudaError_t z_crop(const CropArgs& ca, const float2* tw, int conj, cudaStream_t st) {
+  const int nl = ca.g.n[0] * ca.g.n[1];
+  const unsigned nb = (nl + kF256Lines - 1) / kF256Lines;
+  auto k = f256_z_crop_kernel<3, kModes>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
+  if (e != cudaSuccess) return e;
+  k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, conj);
+  return cudaGetLastError();
+}
+
+F256Lines y_lines(float2* fine, const Geom& g, const float2* tw, int in_prune, int conj) {
   F256Lines y{};
-  y.data = pa.fine;
+  y.data = fine;
   y.G = g.G;
   y.line_stride = 256;
   y.outer_stride = 256 * 256;
   y.outer_modes = 1;
   y.n_outer = g.n[0];
   y.n_axis = g.n[1];
-  y.in_prune = 1;
-  y.out_prune = 0;
+  y.in_prune = in_prune;
+  y.out_prune = !in_prune;
   y.conj = conj;
   y.tw = tw;
-  lines(y, dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
-  F256Lines x = y;
-  x.line_stride = 256 * 256;
-  x.outer_stride = 256;
-  x.outer_modes = 0;
-  x.n_outer = 256;
-  x.n_axis = g.n[0];
-  lines(x, dim3(256 / kF256Lines, 256, pa.ntr), st);
-  return cudaGetLastError();
+  return y;
 }
 
-cudaError_t launch_fft256_adj(const CropArgs& ca, float2* fine, const float2* tw, int isign,
-                              cudaStream_t st) {
-  const Geom& g = ca.g;
-  const int conj = isign > 0;
+F256Lines x_lines(float2* fine, const Geom& g, const float2* tw, int in_prune, int conj) {
   F256Lines x{};
   x.data = fine;
   x.G = g.G;
@@ -430,60 +453,44 @@ cudaError_t launch_fft256_adj(const CropArgs& ca, float2* fine, const float2* tw
   x.outer_modes = 0;
   x.n_outer = 256;
   x.n_axis = g.n[0];
-  x.in_prune = 0;
-  x.out_prune = 1;
+  x.in_prune = in_prune;
+  x.out_prune = !in_prune;
   x.conj = conj;
   x.tw = tw;
-  lines(x, dim3(256 / kF256Lines, 256, ca.ntr), st);
-  F256Lines y = x;
-  y.line_stride = 256;
-  y.outer_stride = 256 * 256;
-  y.outer_modes = 1;
-  y.n_outer = g.n[0];
-  y.n_axis = g.n[1];
-  lines(y, dim3(256 / kF256Lines, g.n[0], ca.ntr), st);
-  const int nl = g.n[0] * g.n[1];
-  const unsigned nb = (nl + kF256Lines - 1) / kF256Lines;
-  // coil sums in shared memory: 3 CTAs per SM (69 against 86 us with the
-  // sums in registers at 2 CTAs per SM, 4 coils of a 128^3 image)
-  auto k = f256_z_crop_kernel<3>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
-  if (e != cudaSuccess) return e;
-  k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, conj);
+  return x;
+}
+}  // namespace
+
+cudaError_t launch_fft256_op(const PadArgs& pa, const float2* tw, int isign, cudaStream_t st) {
+  const Geom& g = pa.g;
+  const int conj = isign > 0;
+  pad_z(pa, tw, conj, st);
+  lines(y_lines(pa.fine, g, tw, 1, conj), dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
+  lines(x_lines(pa.fine, g, tw, 1, conj), dim3(256 / kF256Lines, 256, pa.ntr), st);
   return cudaGetLastError();
+}
+
+cudaError_t launch_fft256_adj(const CropArgs& ca, float2* fine, const float2* tw, int isign,
+                              cudaStream_t st) {
+  const Geom& g = ca.g;
+  const int conj = isign > 0;
+  lines(x_lines(fine, g, tw, 0, conj), dim3(256 / kF256Lines, 256, ca.ntr), st);
+  lines(y_lines(fine, g, tw, 0, conj), dim3(256 / kF256Lines, g.n[0], ca.ntr), st);
+  return z_crop(ca, tw, conj, st);
 }
 
 cudaError_t launch_fft256_gram(const PadArgs& pa, const CropArgs& ca, const float* K,
                                const float2* tw, cudaStream_t st) {
   const Geom& g = pa.g;
-  const int nl = g.n[0] * g.n[1];
-  f256_pad_z_kernel<<<dim3((nl + kF256Lines - 1) / kF256Lines, pa.ntr), kF256Threads, 0, st>>>(
-      pa, tw, 0);
-  F256Lines y{};
-  y.data = pa.fine;
-  y.G = g.G;
-  y.line_stride = 256;
-  y.outer_stride = 256 * 256;
-  y.outer_modes = 1;
-  y.n_outer = g.n[0];
-  y.n_axis = g.n[1];
-  y.in_prune = 1;
-  y.out_prune = 0;
-  y.conj = 0;
-  y.tw = tw;
-  lines(y, dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
-  f256_x_kmul_kernel<<<dim3(256 / kF256Lines, 256), kF256Threads, 0, st>>>(pa.fine, g.G, pa.ntr,
-                                                                            g.n[0], K, tw);
-  y.in_prune = 0;
-  y.out_prune = 1;
-  y.conj = 1;
-  lines(y, dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
-  const unsigned nb = (nl + kF256Lines - 1) / kF256Lines;
-  auto k = f256_z_crop_kernel<3>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
-  if (e != cudaSuccess) return e;
-  k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, 1);
-  return cudaGetLastError();
+  pad_z(pa, tw, 0, st);
+  lines(y_lines(pa.fine, g, tw, 1, 0), dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
+  const dim3 grid(256 / kF256Lines, 256);
+  if (g.n[0] == 128)
+    f256_x_kmul_kernel<kHalf><<<grid, kF256Threads, 0, st>>>(pa.fine, g.G, pa.ntr, g.n[0], K, tw);
+  else
+    f256_x_kmul_kernel<kModes><<<grid, kF256Threads, 0, st>>>(pa.fine, g.G, pa.ntr, g.n[0], K, tw);
+  lines(y_lines(pa.fine, g, tw, 0, 1), dim3(256 / kF256Lines, g.n[0], pa.ntr), st);
+  return z_crop(ca, tw, 1, st);
 }
 
 }  // namespace gbn
