@@ -10,7 +10,8 @@ voxel subsets, for an even 128^3 image and for odd / even 127 x 126 x 128
 (whose modes sit asymmetrically on the 256-point axes; integer modes
 -(N//2) .. N - N//2 - 1, the oracle's "finufft" grid), SENSE and
 calibrationless, with two coil passes (5 coils, 4 per pass), and for the +1
-exponent sign.
+exponent sign; at oversampling 2.5 and 1.25 (101-204 modes on the 256-point
+axes) it is as accurate as the cuFFT path against the oracle.
 """
 
 import numpy as np
@@ -107,3 +108,36 @@ def test_fused_plus_sign_and_trajectory_gradient(gpu_pkg, monkeypatch):
     rows = np.arange(0, M, 37)
     ref = np.conj(ndft.ndft_type2(ku[rows], np.conj(x[0].astype(np.complex128) * smaps[1]), shape))
     assert rel_l2(res[0][0][0, 1, rows], ref) < TOL
+
+
+@pytest.mark.parametrize("shape,osf", [((102, 101, 102), 2.5), ((204, 203, 204), 1.25)])
+def test_fused_other_oversampling(gpu_pkg, monkeypatch, shape, osf):
+    """Other oversampling factors that land on 256-point fine axes: 101-102
+    modes per axis at 2.5 (kernel width 6) and 203-204 at 1.25 (width 10),
+    where a pruned line reads most of its entries.  At 1.25 the
+    deapodisation factors at the band edge are large, so the FP32 rounding
+    of either transform is amplified and the two paths differ by about 1e-4;
+    the criterion is the FP64 oracle: on row and voxel subsets the fused
+    path is as accurate as the cuFFT path (and within 1e-4 at 2.5)."""
+    C, M = 3, 20000
+    k, smaps, x, y, _ = _problem(shape, C, M, seed=int(osf * 100))
+    ops = []
+    for env in ("1", "0"):
+        monkeypatch.setenv("GBN_FUSED_FFT", env)
+        ops.append(gpu_pkg.MRIGB300(k, shape, n_coils=C, smaps=smaps, upsampfac=osf, squeeze_dims=False))
+    monkeypatch.delenv("GBN_FUSED_FFT")
+    assert ops[0].plan.info()["nf"] == (256, 256, 256)
+    ku = ndft.proper_trajectory_unit(k)
+    nrm = ndft.norm_factor(shape)
+    rng = np.random.default_rng(5)
+    rows = np.sort(rng.choice(M, 256, replace=False))
+    ref = ndft.ndft_type2(ku[rows], x[0].astype(np.complex128) * smaps[1], shape, grid="finufft") / nrm
+    err_op = [rel_l2(o.op(x)[0, 1, rows], ref) for o in ops]
+    idx = [np.sort(rng.choice(n, 8, replace=False)) for n in shape]
+    t1 = ndft.ndft_type1_grid(ku, y[0].astype(np.complex128), shape, idx, grid="finufft") / nrm
+    sub = np.ix_(*idx)
+    ref_adj = sum(np.conj(smaps[c][sub]) * t1[c] for c in range(C))
+    err_adj = [rel_l2(o.adj_op(y)[0, 0][sub], ref_adj) for o in ops]
+    for fused, plain in (err_op, err_adj):
+        assert fused <= 1.5 * plain + 1e-6, (fused, plain)
+        assert fused < (TOL if osf == 2.5 else 1e-3), fused
