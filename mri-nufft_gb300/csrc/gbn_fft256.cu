@@ -71,16 +71,40 @@ __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2&
   a3 = make_float2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
 }
 
-// 16-point DFT, exponent sign -1: x[n] in natural order in, X[k] at x[pos16(k)] out
+// 4-point DFT whose inputs a1, a2 are zero (not read)
+__device__ __forceinline__ void dft4_in03(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 p = a0, q = a3;
+  a0 = f2add(p, q);
+  a2 = f2sub(p, q);
+  a1 = make_float2(p.x - q.y, p.y + q.x);  // p + i q
+  a3 = make_float2(p.x + q.y, p.y - q.x);  // p - i q
+}
+
+// 4-point DFT of which only the outputs a0, a3 are used (a1, a2 are left stale)
+__device__ __forceinline__ void dft4_out03(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 t0 = f2add(a0, a2), t1 = f2sub(a0, a2), t2 = f2add(a1, a3), t3 = f2sub(a1, a3);
+  a0 = f2add(t0, t2);
+  a3 = make_float2(t1.x - t3.y, t1.y + t3.x);
+}
+
+// 16-point DFT, exponent sign -1: x[n] in natural order in, X[k] at x[pos16(k)] out.
+// HALF_IN: x[4 .. 11] are zero and not read (the inputs of a 128-mode axis,
+// n = 16 q + b with q < 4 or q >= 12); HALF_OUT: only X[k], k < 4 or k >= 12,
+// are computed (the outputs such an axis keeps).  The IEEE arithmetic does
+// not let the compiler drop additions of constant zeros by itself.
 __device__ __forceinline__ int pos16(int k) { return 4 * (k & 3) + (k >> 2); }
 
+template <bool HALF_IN = false, bool HALF_OUT = false>
 __device__ __forceinline__ void dft16(float2 (&x)[16]) {
   // W16^k = (cos(2 pi k / 16), -sin(2 pi k / 16))
   constexpr float c1 = 0.92387953251128674f;  // cos(pi / 8)
   constexpr float s1 = 0.38268343236508977f;  // sin(pi / 8)
   constexpr float r2 = 0.70710678118654752f;  // sqrt(1 / 2)
 #pragma unroll
-  for (int r = 0; r < 4; ++r) dft4(x[r], x[r + 4], x[r + 8], x[r + 12]);
+  for (int r = 0; r < 4; ++r) {
+    if (HALF_IN) dft4_in03(x[r], x[r + 4], x[r + 8], x[r + 12]);
+    else dft4(x[r], x[r + 4], x[r + 8], x[r + 12]);
+  }
   // x[r + 4 s] *= W16^(r s)
   x[5] = f2mul(x[5], make_float2(c1, -s1));    // r 1, s 1
   x[9] = f2mul(x[9], make_float2(r2, -r2));    // r 1, s 2
@@ -92,7 +116,10 @@ __device__ __forceinline__ void dft16(float2 (&x)[16]) {
   x[11] = f2mul(x[11], make_float2(-r2, -r2)); // r 3, s 2: W16^6
   x[15] = f2mul(x[15], make_float2(-c1, s1));  // r 3, s 3: W16^9
 #pragma unroll
-  for (int s = 0; s < 4; ++s) dft4(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+  for (int s = 0; s < 4; ++s) {
+    if (HALF_OUT) dft4_out03(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+    else dft4(x[4 * s], x[4 * s + 1], x[4 * s + 2], x[4 * s + 3]);
+  }
 }
 
 // modes of an n-point axis on the 256-point fine axis
@@ -166,7 +193,7 @@ f256_pad_z_kernel(PadArgs a, const float2* __restrict__ tw, int conj) {
     x[q] = v;
   }
   __syncthreads();  // twiddle table
-  dft16(x);
+  dft16<SET == kHalf>(x);
   float2* row = s_x + l * (16 * 17);
 #pragma unroll
   for (int k1 = 0; k1 < 16; ++k1) row[k1 * 17 + b] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
@@ -222,14 +249,14 @@ __global__ void __launch_bounds__(kF256Threads, MINB) f256_lines_kernel(F256Line
     x[q] = v;
   }
   __syncthreads();  // twiddle table
-  dft16(x);
+  dft16<IN == kHalf>(x);
 #pragma unroll
   for (int k1 = 0; k1 < 16; ++k1) s_x[(k1 * 16 + b) * 16 + l] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
   __syncthreads();
   const int k1 = b;
 #pragma unroll
   for (int q = 0; q < 16; ++q) x[q] = s_x[(k1 * 16 + q) * 16 + l];
-  dft16(x);
+  dft16<false, OUT == kHalf>(x);
 #pragma unroll
   for (int k2 = 0; k2 < 16; ++k2) {
     if (entry_on<OUT>(k2, k1, a.n_axis)) {
@@ -285,7 +312,7 @@ f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 16; ++q) x[q] = row[k1 * 17 + q];
-    dft16(x);
+    dft16<false, SET == kHalf>(x);
     if (!valid) continue;
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) {
@@ -328,7 +355,7 @@ f256_z_crop_kernel(CropArgs a, const float2* __restrict__ tw, int conj) {
 // transform's first step for b = k1, so the two transforms share one layout.
 // blockIdx.x: 16 consecutive z columns; blockIdx.y: y
 template <int SET>
-__global__ void __launch_bounds__(kF256Threads, 3)
+__global__ void __launch_bounds__(kF256Threads, 4)
 f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __restrict__ K,
                    const float2* __restrict__ tw) {
   __shared__ float2 s_tw[256];
@@ -348,7 +375,7 @@ f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __rest
     for (int q = 0; q < 16; ++q)
       x[q] = entry_on<SET>(q, b, n0) ? base[(16 * q + b) * XS] : make_float2(0.f, 0.f);
     __syncthreads();  // twiddles; the previous transform's exchange reads are done
-    dft16(x);
+    dft16<SET == kHalf>(x);
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) s_x[(k1 * 16 + b) * 16 + l] = f2mul(x[pos16(k1)], s_tw[k1 * 16 + b]);
     __syncthreads();
@@ -366,7 +393,7 @@ f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __rest
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 16; ++q) y[q] = s_x[(b * 16 + q) * 16 + l];
-    dft16(y);
+    dft16<false, SET == kHalf>(y);
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2)
       if (entry_on<SET>(k2, b, n0)) base[(b + 16 * k2) * XS] = f2conj(y[pos16(k2)]);
