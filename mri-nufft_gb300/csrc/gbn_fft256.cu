@@ -20,9 +20,16 @@
 //           z lines of the (x mode, y mode) columns (all in, mode entries
 //           out), crop fused into the stores (divide by phihat, scale, and
 //           the SENSE coil combine sum_c conj(s_c) v_c over the pass's coils).
+//   Toeplitz Gram (256^3 circulant grid): the op's z and y passes, one pass
+//           over the (y, z) lines doing the forward x transform, the
+//           multiply by the spectrum and the inverse x transform, then the
+//           adjoint's y and z passes.
 //
 // For a 128^3 image this moves about 350 MB per coil and transform against
-// about 670 MB for the pad pass plus the pruned cuFFT passes.
+// about 670 MB for the pad pass plus the pruned cuFFT passes.  For 128-point
+// image axes the entries of a line that hold modes are whole rows of the
+// four-step layout (q < 4 and q >= 12 below), a compile-time set (kHalf);
+// other sizes test each entry at run time (kModes).
 //
 // A 256-point line transform is two 16-point DFTs in registers with one
 // exchange through shared memory (four-step: n = 16 a + b, k = k1 + 16 k2):
