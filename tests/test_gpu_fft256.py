@@ -141,3 +141,27 @@ def test_fused_other_oversampling(gpu_pkg, monkeypatch, shape, osf):
     for fused, plain in (err_op, err_adj):
         assert fused <= 1.5 * plain + 1e-6, (fused, plain)
         assert fused < (TOL if osf == 2.5 else 1e-3), fused
+
+
+@pytest.mark.parametrize("sense", [True, False])
+def test_fused_several_batches(gpu_pkg, monkeypatch, sense):
+    """n_batchs = 2: the passes loop over batch items (SENSE: one image per
+    item, its crop restarts the coil sum); op, adjoint, data consistency and
+    the Toeplitz Gram against the cuFFT path."""
+    shape, C, B, M = (128, 128, 128), 3, 2, 20000
+    rng = np.random.default_rng(21 + sense)
+    k, smaps, _, _, dens = _problem(shape, C, M, seed=31 + sense)
+    cpx = lambda *s: (rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64)
+    x = cpx(B, 1, *shape) if sense else cpx(B, C, *shape)
+    y = cpx(B, C, M)
+    ops = []
+    for env in ("1", "0"):
+        monkeypatch.setenv("GBN_FUSED_FFT", env)
+        ops.append(gpu_pkg.MRIGB300(k, shape, n_coils=C, n_batchs=B, smaps=smaps if sense else None,
+                                    density=dens, squeeze_dims=False))
+    monkeypatch.delenv("GBN_FUSED_FFT")
+    assert rel_l2(ops[0].op(x), ops[1].op(x)) < SAME
+    assert rel_l2(ops[0].adj_op(y), ops[1].adj_op(y)) < SAME
+    assert rel_l2(ops[0].data_consistency(x, y), ops[1].data_consistency(x, y)) < SAME
+    if sense:
+        assert rel_l2(ops[0].gram_op(x), ops[1].gram_op(x)) < SAME
