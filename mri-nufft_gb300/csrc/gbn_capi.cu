@@ -21,6 +21,7 @@
 
 #include "gbn_batch.cuh"
 #include "gbn_fft256.cuh"
+#include "gbn_fft512.cuh"
 #include "gbn_internal.cuh"
 #include "gbn_passes.cuh"
 #include "gbn_sort.cuh"
@@ -199,6 +200,10 @@ struct gbn_plan_s {
   // replace the pad pass, cuFFT and the crop pass of op / adj / dc
   bool fft256 = false;
   float2* tw256 = nullptr;  // W256^k table
+  // 512^2 fine grids (2D): the same with the 512-point line transforms of
+  // gbn_fft512.cu
+  bool fft512 = false;
+  float2* tw512 = nullptr;  // W512^(b k1) table
 
   // per-stage CUDA-event timing (gbn_profile) and kernel launch count
   bool prof = false;
@@ -226,6 +231,7 @@ struct gbn_plan_s {
     dev_free(fine);
     dev_free(kbuf);
     dev_free(tw256);
+    dev_free(tw512);
     free_points();
     free_bins();
     dev_free(sb.d_total);
@@ -442,6 +448,12 @@ void run_crop(gbn_plan p, const CropArgs& a, cudaStream_t st) {
 }
 // op: pad + forward transform (fused line transforms on 256^3 grids)
 void run_pad_fft(gbn_plan p, const PadArgs& a, int isign, cudaStream_t st) {
+  if (p->fft512) {
+    Span span(p, GBN_STAGE_FFT, st);
+    ck(launch_fft512_op(a, p->tw512, isign, st), "fused pad + transform");
+    p->launches += 2;
+    return;
+  }
   if (p->fft256) {
     Span span(p, GBN_STAGE_FFT, st);
     ck(launch_fft256_op(a, p->tw256, isign, st), "fused pad + transform");
@@ -453,6 +465,13 @@ void run_pad_fft(gbn_plan p, const PadArgs& a, int isign, cudaStream_t st) {
 }
 // adjoint: inverse transform + crop
 void run_fft_crop(gbn_plan p, const CropArgs& a, int isign, cudaStream_t st) {
+  if (p->fft512) {
+    Span span(p, GBN_STAGE_FFT, st);
+    ck(launch_fft512_adj(a, const_cast<float2*>(a.fine), p->tw512, isign, st),
+       "fused transform + crop");
+    p->launches += 2;
+    return;
+  }
   if (p->fft256) {
     Span span(p, GBN_STAGE_FFT, st);
     ck(launch_fft256_adj(a, p->fine, p->tw256, isign, st), "fused transform + crop");
@@ -692,6 +711,14 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
         p->tw256 = dev_alloc<float2>(256, p->bytes, "transform twiddles");
         ck(cudaMemcpy(p->tw256, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice),
            "copy transform twiddles");
+      }
+      p->fft512 = !spread_only && fft512_fits(g) && !(f && std::atoi(f) == 0);
+      if (p->fft512) {
+        std::vector<float> t = fft512_twiddles();
+        p->tw512 = dev_alloc<float2>(512, p->bytes, "transform twiddles");
+        ck(cudaMemcpy(p->tw512, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice),
+           "copy transform twiddles");
+        ck(fft512_prepare(), "transform kernel attributes");
       }
     }
     p->fine = dev_alloc<float2>((size_t)ntrans * g.G, p->bytes, "fine grid");
@@ -1208,6 +1235,12 @@ void toep_apply(gbn_toep t, const void* img, const void* smaps, void* out, int B
       Span span(p, GBN_STAGE_FFT, st);
       ck(launch_fft256_gram(pa, ca, t->K, p->tw256, st), "fused Toeplitz Gram");
       p->launches += 5;
+      return;
+    }
+    if (p->fft512) {
+      Span span(p, GBN_STAGE_FFT, st);
+      ck(launch_fft512_gram(pa, ca, t->K, p->tw512, st), "fused Toeplitz Gram");
+      p->launches += 3;
       return;
     }
     run_pad_fft(p, pa, -1, st);
