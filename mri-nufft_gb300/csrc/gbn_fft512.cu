@@ -129,9 +129,11 @@ constexpr size_t kYSmem = (512 + kL * 32 * 17) * sizeof(float2);   // twiddles +
 constexpr size_t kXSmem = (512 + 32 * 16 * kL) * sizeof(float2);
 
 // ---------------------------------------------------------------- y lines, pad fused
-// blockIdx.x: 16 consecutive x image rows; blockIdx.y: transform.  SET: the y modes.
+// blockIdx.x: 16 consecutive x image rows; blockIdx.y: transform.  SET: the y
+// modes.  3 CTAs per SM (80 registers): 23.5 against 26.9 us at 2 CTAs and
+// 126 registers for 64 transforms; the other kernels measured slower at 3.
 template <int SET>
-__global__ void __launch_bounds__(kT, 2)
+__global__ void __launch_bounds__(kT, 3)
 f512_pad_y_kernel(PadArgs a, const float2* __restrict__ tw, int conj) {
   extern __shared__ float2 s_dyn[];
   float2* const s_tw = s_dyn;
