@@ -1581,8 +1581,8 @@ spread_stream2d_kernel(SpreadArgs a) {
 // weights, flush rules and transforms per warp are those of the column
 // kernel; the rows both halves own are flushed by both.
 // ---------------------------------------------------------------------------
-template <int W, int CG>
-__global__ void __launch_bounds__(GBN_THREADS, 2)
+template <int W, int CG, int MINB = 2>
+__global__ void __launch_bounds__(GBN_THREADS, MINB)
 spread_half2d_kernel(SpreadArgs a) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const int nw = blockDim.x >> 5;
@@ -1734,7 +1734,11 @@ cudaError_t launch_spread_half2d_t(const SpreadArgs& a, cudaStream_t st) {
   const int passes = (a.ntr + nw * CG - 1) / (nw * CG);
   if (passes > 65535) return cudaErrorInvalidValue;
   const size_t smem = stream2_smem_bytes(nw * CG) + 2 * kStream2Batch * sizeof(short);
-  auto k = spread_half2d_kernel<W, CG>;
+  // full 256-thread CTAs at 3 per SM (80 registers, 32 bytes of spills):
+  // stack-of-stars spread 6.30 against 6.67 ms; CTAs of fewer warps keep 2
+  // (104 registers, no spills; the 8-coil differentiable step measured 5 %
+  // slower with the spills)
+  auto k = nw == GBN_THREADS / 32 ? spread_half2d_kernel<W, CG, 3> : spread_half2d_kernel<W, CG, 2>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<dim3(a.s.nsub, passes), nw * 32, smem, st>>>(a);
