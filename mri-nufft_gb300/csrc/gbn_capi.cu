@@ -711,6 +711,7 @@ int gbn_plan_create(int dim, const int64_t* n_modes, double upsampfac, double ep
         p->tw256 = dev_alloc<float2>(256, p->bytes, "transform twiddles");
         ck(cudaMemcpy(p->tw256, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice),
            "copy transform twiddles");
+        ck(fft256_prepare(), "transform kernel attributes");
       }
       p->fft512 = !spread_only && fft512_fits(g) && !(f && std::atoi(f) == 0);
       if (p->fft512) {

@@ -344,6 +344,11 @@ f256_x_kmul_kernel(float2* data, int64_t G, int ntr, int n0, const float* __rest
 
 }  // namespace
 
+cudaError_t fft256_prepare() {
+  return cudaFuncSetAttribute(f256_z_crop_kernel<3, kModes>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
+}
+
 bool fft256_fits(const Geom& g) {
   return g.dim == 3 && g.nf[0] == 256 && g.nf[1] == 256 && g.nf[2] == 256;
 }
@@ -390,10 +395,7 @@ void pad_z(const PadArgs& pa, const float2* tw, int conj, cudaStream_t st) {
 cudaError_t z_crop(const CropArgs& ca, const float2* tw, int conj, cudaStream_t st) {
   const int nl = ca.g.n[0] * ca.g.n[1];
   const unsigned nb = (nl + kF256Lines - 1) / kF256Lines;
-  auto k = f256_z_crop_kernel<3, kModes>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCropSmem);
-  if (e != cudaSuccess) return e;
-  k<<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, conj);
+  f256_z_crop_kernel<3, kModes><<<nb, kF256Threads, kCropSmem, st>>>(ca, tw, conj);
   return cudaGetLastError();
 }
 

@@ -11,8 +11,12 @@ namespace gbn {
 // 3D plans whose fine grid is 256 on every axis
 bool fft256_fits(const Geom& g);
 
-// W256^k = exp(-2 pi i k / 256), k = 0 .. 255, as 512 floats (re, im)
+// W256^(b k1), entry k1 * 16 + b (k1, b < 16), as 512 floats (re, im)
 std::vector<float> fft256_twiddles();
+
+// raises the dynamic shared-memory limit of the crop kernel (once, outside
+// any stream capture)
+cudaError_t fft256_prepare();
 
 // op: pad (pa: image, coil maps, 1/phihat, scale) and the pruned transform
 // of sign isign into pa.fine (pa.ntr grids); every fine cell is written.
