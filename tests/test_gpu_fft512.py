@@ -130,3 +130,13 @@ def test_fused_other_oversampling(gpu_pkg, monkeypatch, shape, osf):
     for fused, plain in (err_op, err_adj):
         assert fused <= 1.5 * plain + 1e-6, (fused, plain)
         assert fused < (TOL if osf == 2.5 else 1e-3), fused
+
+
+def test_fused_many_coils(gpu_pkg, monkeypatch):
+    """24 coils in one pass (one launch per pass direction over all coils)."""
+    shape, C, M = (256, 256), 24, 20000
+    k, smaps, xs, xc, y, dens = _problem(shape, C, M, seed=40)
+    fused, plain = _pair(gpu_pkg, monkeypatch, k, shape, n_coils=C, smaps=smaps, density=dens)
+    assert rel_l2(fused.op(xs), plain.op(xs)) < SAME
+    assert rel_l2(fused.adj_op(y), plain.adj_op(y)) < SAME
+    assert rel_l2(fused.gram_op(xs), plain.gram_op(xs)) < SAME
