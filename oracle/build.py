@@ -28,6 +28,8 @@ def build(force: bool = False) -> Path:
         obj = OUT / f"esnufft{suffix}.o"
         cmd = [cc, "-O3", "-fopenmp", "-fPIC", "-std=c11", f"-DREAL={real}", f"-DSUFFIX={suffix}",
                "-D_DEFAULT_SOURCE", "-c", str(SRC), "-o", str(obj)]
+        if real == "float":
+            cmd.insert(-4, "-DREAL_IS_FLOAT")
         subprocess.run(cmd, check=True)
         objs.append(str(obj))
     tmp = LIB.with_suffix(".so.tmp")
