@@ -68,6 +68,72 @@ static inline double fold(double k, int64_t nf) {
   return u;
 }
 
+#ifdef REAL_IS_FLOAT
+/* The float build evaluates the kernel from a piecewise polynomial, as the
+ * single-precision library does: cell t of a footprint sees
+ * phi(s - w/2 + t) with s = x0 + w/2 in [0, 1), which is interpolated at
+ * NPOLY Chebyshev nodes of [0, 1) and stored as a power series in 2s - 1
+ * (double coefficients, Horner in double).  Interior cells fit to ~1e-11,
+ * the two edge cells to ~1.5e-7 (the square-root edge of the support). */
+#define NPOLY(w) ((w) + 4)
+typedef struct {
+  int n;
+  double c[MAXW][MAXW + 5];
+} Poly;
+
+static void poly_fit(int w, double beta, Poly* P) {
+  const int n = NPOLY(w) > MAXW + 4 ? MAXW + 4 : NPOLY(w);
+  P->n = n;
+  double xk[MAXW + 5], tk[MAXW + 5][MAXW + 5];
+  for (int k = 0; k < n; ++k) xk[k] = cos(M_PI * (k + 0.5) / n);
+  for (int t = 0; t < w; ++t) {
+    double f[MAXW + 5], ch[MAXW + 5];
+    for (int k = 0; k < n; ++k) {
+      const double z = ((0.5 * (xk[k] + 1.0)) - 0.5 * w + t) * 2.0 / w;
+      const double q = 1.0 - z * z;
+      f[k] = q > 0 ? exp(beta * (sqrt(q) - 1.0)) : 0.0;
+    }
+    for (int j = 0; j < n; ++j) { /* Chebyshev coefficients at the nodes */
+      double a = 0;
+      for (int k = 0; k < n; ++k) a += f[k] * cos(M_PI * j * (k + 0.5) / n);
+      ch[j] = (j == 0 ? 1.0 : 2.0) * a / n;
+    }
+    /* power series: T_0 = 1, T_1 = x, T_{j+1} = 2 x T_j - T_{j-1} */
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) tk[j][i] = 0;
+    tk[0][0] = 1;
+    if (n > 1) tk[1][1] = 1;
+    for (int j = 1; j + 1 < n; ++j)
+      for (int i = 0; i < n; ++i)
+        tk[j + 1][i] = (i > 0 ? 2 * tk[j][i - 1] : 0) - tk[j - 1][i];
+    for (int i = 0; i < n; ++i) {
+      double a = 0;
+      for (int j = 0; j < n; ++j) a += ch[j] * tk[j][i];
+      P->c[t][i] = a;
+    }
+  }
+}
+
+static inline void weights_poly(double u, int w, const Poly* P, int64_t* i0, REAL* wt) {
+  const double s = u - 0.5 * w;
+  const int64_t a = (int64_t)ceil(s);
+  const double x = 2.0 * ((double)a - u + 0.5 * w) - 1.0;
+  for (int t = 0; t < w; ++t) {
+    double v = P->c[t][P->n - 1];
+    for (int i = P->n - 2; i >= 0; --i) v = v * x + P->c[t][i];
+    wt[t] = (REAL)v;
+  }
+  *i0 = a;
+}
+#define WEIGHTS(u, w, beta, i0, wt) weights_poly((u), (w), &poly, (i0), (wt))
+#define POLY_SETUP(w, beta) \
+  Poly poly;                \
+  poly_fit((w), (beta), &poly)
+#else
+#define WEIGHTS(u, w, beta, i0, wt) weights((u), (w), (beta), (i0), (wt))
+#define POLY_SETUP(w, beta) (void)0
+#endif
+
 static inline void weights(double u, int w, double beta, int64_t* i0, REAL* wt) {
   double s = u - 0.5 * w;
   int64_t a = (int64_t)ceil(s);
@@ -134,6 +200,7 @@ void FN(es_interp)(int dim, const int64_t* nf, int64_t M, const REAL* k0, const 
   int64_t nb[3], *order, *start;
   bin_sort(dim, nf, M, k0, k1, k2, dim == 3 ? BIN3 : BIN2, nb, &order, &start);
   free(start);
+  POLY_SETUP(w, beta);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 1024)
@@ -142,8 +209,8 @@ void FN(es_interp)(int dim, const int64_t* nf, int64_t M, const REAL* k0, const 
     const int64_t j = order[q];
     REAL w0[MAXW], w1[MAXW], w2[MAXW];
     int64_t a0, a1, a2 = 0, c0[MAXW], c1[MAXW], c2[MAXW];
-    weights(fold(k0[j], nf[0]), w, beta, &a0, w0);
-    weights(fold(k1[j], nf[1]), w, beta, &a1, w1);
+    WEIGHTS(fold(k0[j], nf[0]), w, beta, &a0, w0);
+    WEIGHTS(fold(k1[j], nf[1]), w, beta, &a1, w1);
     axis_cells(a0, w, nf[0], c0);
     int cont1 = axis_cells(a1, w, nf[1], c1);
     double sr = 0, si = 0;
@@ -167,7 +234,7 @@ void FN(es_interp)(int dim, const int64_t* nf, int64_t M, const REAL* k0, const 
         si += w0[t0] * ri;
       }
     } else {
-      weights(fold(k2[j], nf[2]), w, beta, &a2, w2);
+      WEIGHTS(fold(k2[j], nf[2]), w, beta, &a2, w2);
       int cont2 = axis_cells(a2, w, nf[2], c2);
       if (cont2) {
         /* rows of 2w contiguous values: v = sum over (t0, t1) of w0 w1 row,
@@ -271,6 +338,7 @@ void FN(es_spread)(int dim, const int64_t* nf, int64_t M, const REAL* k0, const 
                    const REAL* k2, const REAL* c, REAL* grid, int w, double beta, int nthreads) {
   int64_t bs = dim == 3 ? BIN3 : BIN2;
   if (bs < w + 2) bs = w + 2;
+  POLY_SETUP(w, beta);
   int64_t nb[3], *order, *start;
   const int64_t nbins = bin_sort(dim, nf, M, k0, k1, k2, bs, nb, &order, &start);
   /* padded subgrid: bin origin - (w + 1) / 2, extent bs + w + 2 per spread axis */
@@ -318,12 +386,12 @@ void FN(es_spread)(int dim, const int64_t* nf, int64_t M, const REAL* k0, const 
           if (n < DENSE) { /* straight into the fine grid */
             for (int64_t q = start[b]; q < start[b + 1]; ++q) {
               const int64_t j = order[q];
-              weights(fold(k0[j], nf[0]), w, beta, &a[0], w0);
-              weights(fold(k1[j], nf[1]), w, beta, &a[1], w1);
+              WEIGHTS(fold(k0[j], nf[0]), w, beta, &a[0], w0);
+              WEIGHTS(fold(k1[j], nf[1]), w, beta, &a[1], w1);
               axis_cells(a[0], w, nf[0], c0);
               axis_cells(a[1], w, nf[1], c1);
               if (dim == 3) {
-                weights(fold(k2[j], nf[2]), w, beta, &a[2], w2);
+                WEIGHTS(fold(k2[j], nf[2]), w, beta, &a[2], w2);
                 axis_cells(a[2], w, nf[2], c2);
               }
               spread_cells(dim, nf, c0, c1, c2, w0, w1, w2, c[2 * j], c[2 * j + 1], grid, w);
@@ -342,14 +410,14 @@ void FN(es_spread)(int dim, const int64_t* nf, int64_t M, const REAL* k0, const 
           }
           for (int64_t q = start[b]; q < start[b + 1]; ++q) {
             const int64_t j = order[q];
-            weights(fold(k0[j], nf[0]), w, beta, &a[0], w0);
-            weights(fold(k1[j], nf[1]), w, beta, &a[1], w1);
+            WEIGHTS(fold(k0[j], nf[0]), w, beta, &a[0], w0);
+            WEIGHTS(fold(k1[j], nf[1]), w, beta, &a[1], w1);
             for (int t = 0; t < w; ++t) {
               c0[t] = a[0] - o[0] + t;
               c1[t] = a[1] - o[1] + t;
             }
             if (dim == 3) {
-              weights(fold(k2[j], nf[2]), w, beta, &a[2], w2);
+              WEIGHTS(fold(k2[j], nf[2]), w, beta, &a[2], w2);
               for (int t = 0; t < w; ++t) c2[t] = a[2] - o[2] + t;
             }
             spread_cells(dim, ln, c0, c1, c2, w0, w1, w2, c[2 * j], c[2 * j + 1], s, w);
