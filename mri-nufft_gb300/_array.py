@@ -88,8 +88,18 @@ def from_tensor(t: torch.Tensor, like: Interface):
     if like.kind == "cai":
         return t
     if PINNED_RESULTS and t.is_cuda:
-        out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-        out.copy_(t, non_blocking=True)
-        torch.cuda.current_stream(t.device).synchronize()
-        return out.numpy()
+        out = pinned_empty(t.shape, t.dtype)
+        if out is not None:
+            out.copy_(t, non_blocking=True)
+            torch.cuda.current_stream(t.device).synchronize()
+            return out.numpy()
     return t.cpu().numpy()
+
+
+def pinned_empty(shape, dtype):
+    """A page-locked host tensor, or None when the host cannot lock that much
+    memory (the caller then falls back to pageable memory)."""
+    try:
+        return torch.empty(shape, dtype=dtype, pin_memory=True)
+    except RuntimeError:
+        return None

@@ -361,9 +361,11 @@ class MRIGB300(_Base):
         """op of a numpy image: groups of coils, the device-to-host copy of a
         group's k-space overlapping the next group's transforms."""
         B, C, M = self.n_batchs, self.n_coils, self.n_samples
+        out = _array.pinned_empty((B, C, M), torch.complex64)
+        if out is None:  # the host cannot lock that much memory: one call, pageable copy
+            return _array.from_tensor(self._op_device(self._img_tensor(data)), _array.Interface("numpy"))
         x = self._img_tensor(data)
         dev_k = torch.empty((B, C, M), dtype=torch.complex64, device=self.device)
-        out = torch.empty((B, C, M), dtype=torch.complex64, pin_memory=True)
         main = torch.cuda.current_stream(self.device)
         side = self._copy_stream()
         for b in range(B):
